@@ -1,0 +1,161 @@
+/*
+ * parrsb.h -- drop-in C ABI of the GB300 partitioning library.
+ *
+ * The two entry points keep the names, argument order, argument meaning,
+ * ownership rules and return codes of parRSB's public header
+ * (src/parRSB.h:21-48 and src/parRSB.h:62-70).  The one change is the
+ * communicator: an MPI_Comm argument becomes an explicit part count
+ * (`nparts`), because the whole mesh lives on one GPU and the reference's
+ * "one MPI rank per part" becomes "one virtual rank per part".
+ *
+ * All pointers are caller-owned HOST memory unless an entry point's name
+ * ends in `_device`, in which case they are device pointers on the current
+ * CUDA device.  Outputs are written only on success (return value 0).
+ *
+ * Return codes (the reference returns 0 / 1 / the gencon check error and
+ * otherwise aborts the process; this library never exits):
+ *   PARRSB_OK            0  success
+ *   PARRSB_ERR_ARGS      1  bad arguments (also: tagged == 1 with tag NULL,
+ *                           as in src/parrsb.c:873-877; gencon: element or
+ *                           face check failed, as in src/con.c:238-257)
+ *   PARRSB_ERR_CUDA      2  a CUDA call failed (message on stderr)
+ *   PARRSB_ERR_CHECK     3  an internal consistency check failed
+ *   PARRSB_ERR_UNSUPPORTED 4 option outside the GPU path (tagged
+ *                           partitioning, rsb_algo = 1 multigrid, periodic
+ *                           faces in gencon)
+ */
+#ifndef PARRSB_GB300_H
+#define PARRSB_GB300_H
+
+#if defined(__GNUC__)
+#define PARRSB_API __attribute__((visibility("default")))
+#else
+#define PARRSB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PARRSB_OK 0
+#define PARRSB_ERR_ARGS 1
+#define PARRSB_ERR_CUDA 2
+#define PARRSB_ERR_CHECK 3
+#define PARRSB_ERR_UNSUPPORTED 4
+
+/* Byte-identical to parrsb_options in src/parRSB.h:21-41 (14 ints and one
+ * double, same field order).  Environment variables PARRSB_<FIELD> override
+ * the caller's values and are written back into the struct, as in
+ * update_options (src/parrsb.c:48-77). */
+typedef struct {
+  int partitioner;             /* 0 RSB, 1 RCB, 2 RIB (default 0) */
+  int tagged;                  /* tagged partitioning (unsupported here) */
+  int levels;                  /* 1 or 2; clamped to <= 2 (default 2) */
+  int find_disconnected_comps; /* count components per bisection (1) */
+  int repair;                  /* accepted, no effect (as in the reference) */
+  int verbose_level;           /* 0 quiet, >=1 prints options and time (1) */
+  int profile_level;           /* >=1 prints per-level stage times (0) */
+  int rsb_algo;                /* 0 Lanczos (1 = multigrid: unsupported) */
+  int rsb_pre;                 /* 0 none, 1 RCB, 2 RIB pre-partition (1) */
+  int rsb_max_iter;            /* Lanczos steps per restart (50) */
+  int rsb_max_passes;          /* Lanczos restarts (50) */
+  double rsb_tol;              /* Lanczos tolerance (1e-5) */
+  int rsb_dump_stats;          /* accepted, no effect (as in the reference) */
+  int rsb_mg_grammian;         /* multigrid only: accepted, no effect */
+  int rsb_mg_factor;           /* multigrid only: accepted, no effect */
+} parrsb_options;
+
+/* Defaults of src/parrsb.c:26-44. */
+extern PARRSB_API parrsb_options parrsb_default_options;
+
+/* Partition `nel` elements of `nv` vertices (nv == 8: hex, 3D; otherwise
+ * quad, 2D) into `nparts` parts; part[e] receives the part of element e.
+ * Replaces parrsb_part_mesh (src/parRSB.h:45-48, src/parrsb.c:853-906);
+ * `comm` becomes `nparts`.  vtx: nel*nv global vertex ids (may be NULL for
+ * RCB/RIB); xyz: nel*nv*ndim corner coordinates (may be NULL: rsb_pre is then
+ * set to 0, as src/parrsb.c:250 does). */
+PARRSB_API int parrsb_part_mesh(int *part, const long long *vtx, const double *xyz,
+                     const int *tag, int nel, int nv, parrsb_options *options,
+                     int nparts);
+
+/* Tolerance-based vertex numbering ("gencon").  Replaces parrsb_conn_mesh
+ * (src/parRSB.h:62-64, src/con.c:189-295) without the communicator.
+ * coord: nel * nv * nDim doubles, corners in Nek preprocessor order;
+ * vtx: nel * nv output ids in symmetric corner order (1-based, dense).
+ * Returns 1 when the element or face check fails (vtx is then untouched),
+ * 4 when nPeriodicFaces > 0. */
+PARRSB_API int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel,
+                     unsigned nDim, long long *periodicInfo,
+                     int nPeriodicFaces, double tol);
+
+/* Fortran binding of parrsb_conn_mesh (src/parRSB.h:66-70, src/con.c:300-306)
+ * with the communicator argument removed; *err receives the return code. */
+PARRSB_API void fparrsb_conn_mesh(long long *vtx, double *coord, int *nel, int *nDim,
+                       long long *periodicInfo, int *nPeriodicFaces,
+                       double *tol, int *err);
+
+/* ------------------------------------------------------------------------
+ * Extensions (no counterpart in the reference).
+ * ---------------------------------------------------------------------- */
+
+/* Same as parrsb_part_mesh / parrsb_conn_mesh with every array a DEVICE
+ * pointer on the current device (inputs already resident in HBM). */
+PARRSB_API int parrsb_part_mesh_device(int *d_part, const long long *d_vtx,
+                            const double *d_xyz, int nel, int nv,
+                            parrsb_options *options, int nparts);
+PARRSB_API int parrsb_conn_mesh_device(long long *d_vtx, const double *d_coord,
+                            unsigned int nel, unsigned nDim, double tol);
+
+/* Statistics of the last parrsb_part_mesh / parrsb_conn_mesh call on this
+ * thread.  Stage times come from CUDA events; counts from device state. */
+typedef struct {
+  double total_ms;        /* whole call, host-measured */
+  double stage_ms[12];    /* see PARRSB_STAGE_* */
+  long long lanczos_iters;    /* sum over all bisections of Lanczos steps */
+  long long lanczos_row_iters;/* sum over bisections of steps * rows */
+  long long spmv_launches;    /* SpMV kernel launches */
+  double spmv_ms;             /* summed CUDA-event time of SpMV launches */
+  long long spmv_bytes;       /* algorithmic bytes moved by those launches */
+  long long kernel_launches;  /* all kernels launched by the call */
+  int levels;                 /* bisection levels run */
+  int max_components;         /* max component count over all halves */
+  double max_fiedler_resid;   /* max FP64 ||Lf - rho f|| / ||f|| (if checked) */
+  int unconverged;            /* bisections that used all restarts */
+  long long nnz;              /* off-diagonal nonzeros of the dual graph */
+  long long gencon_segments;  /* gencon: number of distinct ids */
+} parrsb_stats;
+
+enum {
+  PARRSB_STAGE_UPLOAD = 0,
+  PARRSB_STAGE_SETUP = 1,     /* centroids, dual graph */
+  PARRSB_STAGE_PRE = 2,       /* RCB / RIB pre-partition */
+  PARRSB_STAGE_LANCZOS = 3,
+  PARRSB_STAGE_TQLI = 4,      /* tridiagonal solves + Ritz vectors */
+  PARRSB_STAGE_SORT = 5,      /* Fiedler sort + split */
+  PARRSB_STAGE_COMPONENTS = 6,
+  PARRSB_STAGE_BALANCE = 7,
+  PARRSB_STAGE_RESTRICT = 8,  /* per-level graph restriction */
+  PARRSB_STAGE_DOWNLOAD = 9,
+  PARRSB_STAGE_GENCON = 10,
+  PARRSB_STAGE_CHECK = 11
+};
+
+PARRSB_API int parrsb_get_stats(parrsb_stats *out);
+
+/* Partition quality on the element dual graph (weight = shared vertices):
+ * q[0] weighted edge cut, q[1] cut dual edges, q[2] cut face-sharing pairs,
+ * q[3] max part size, q[4] min part size, q[5] imbalance max*nparts/nel,
+ * q[6] shared-vertex communication volume summed over parts (the `nss`
+ * figure of src/helpers.c:132-224), q[7] max neighbour parts of a part.
+ * Host arrays; computed on the GPU. */
+PARRSB_API int parrsb_part_quality(double *q, const int *part, const long long *vtx,
+                        int nel, int nv, int nparts);
+
+/* Release the device workspace cached by earlier calls on this thread. */
+PARRSB_API void parrsb_gpu_finalize(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARRSB_GB300_H */

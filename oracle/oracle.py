@@ -1,0 +1,177 @@
+"""ctypes wrapper of the C oracle (parrsb_oracle.c).
+
+Test infrastructure only: used by tests/, by ``__graft_entry__.smoke()`` and
+by the CPU-baseline leg of ``bench.py``.  The product library never imports
+this module.  ``build()`` compiles the C restatement with gcc into
+``oracle/_build/`` (no FMA contraction, like the reference's ISO C99 build).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from parrsb_gb300.options import ParrsbOptions
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "parrsb_oracle.c")
+HDR = os.path.join(HERE, "parrsb_oracle.h")
+LIB = os.path.join(HERE, "_build", "libparrsb_oracle.so")
+
+_lib = None
+
+
+def build(force=False):
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    cmd = ["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", LIB + ".tmp", SRC, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class RsbInfo(ctypes.Structure):
+    _fields_ = [("total_iters", ctypes.c_longlong), ("nbisect", ctypes.c_int),
+                ("unconverged", ctypes.c_int), ("max_components", ctypes.c_int),
+                ("max_resid", ctypes.c_double), ("levels", ctypes.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        L.oracle_part_mesh.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ParrsbOptions),
+                                       ctypes.c_int, ctypes.POINTER(RsbInfo)]
+        L.oracle_conn_mesh.argtypes = [P, P, ctypes.c_uint, ctypes.c_uint,
+                                       ctypes.c_double, ctypes.c_int, P, P]
+        L.oracle_centroids.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
+        L.oracle_tree_sum.argtypes = [P, ctypes.c_longlong]
+        L.oracle_tree_sum.restype = ctypes.c_double
+        L.oracle_power_serial.argtypes = [P, ctypes.c_int, P]
+        L.oracle_tqli.argtypes = [P, P, ctypes.c_int, P, P]
+        L.oracle_laplacian.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
+        L.oracle_dual_graph.argtypes = [P, P, P, ctypes.c_longlong, P,
+                                        ctypes.c_int, ctypes.c_int]
+        L.oracle_dual_graph.restype = ctypes.c_longlong
+        L.oracle_components.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
+        L.oracle_part_quality.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int]
+        L.oracle_fiedler.argtypes = [P, P, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def part_mesh(vtx, xyz, nparts, want_order=False, **opts):
+    """Oracle parrsb_part_mesh.  Returns (rc, part, order, info, options)."""
+    nel = len(vtx) if vtx is not None else len(xyz)
+    nv = (vtx.shape[1] if vtx is not None else xyz.shape[1])
+    vtx = None if vtx is None else np.ascontiguousarray(vtx, np.int64)
+    xyz = None if xyz is None else np.ascontiguousarray(xyz, np.float64)
+    opts.setdefault("verbose_level", 0)
+    o = ParrsbOptions.make(**opts)
+    part = np.full(nel, -1, np.int32)
+    order = np.full(nel, -1, np.int32) if want_order else None
+    info = RsbInfo()
+    rc = lib().oracle_part_mesh(_p(part), _p(order), _p(vtx), _p(xyz), nel, nv,
+                                ctypes.byref(o), nparts, ctypes.byref(info))
+    return rc, part, order, info, o
+
+
+def conn_mesh(coord, ndim, tol=0.2, heapsort=False):
+    """Oracle parrsb_conn_mesh.  Returns (rc, vtx, ids, nseg)."""
+    coord = np.ascontiguousarray(coord, np.float64)
+    nv = 4 if ndim == 2 else 8
+    nel = coord.size // (nv * ndim)
+    vtx = np.zeros(nel * nv, np.int64)
+    ids = np.zeros(nel * nv, np.int64)
+    nseg = ctypes.c_longlong(0)
+    rc = lib().oracle_conn_mesh(_p(vtx), _p(coord), nel, ndim, tol,
+                                1 if heapsort else 0, _p(ids),
+                                ctypes.byref(nseg))
+    return rc, vtx.reshape(nel, nv), ids.reshape(nel, nv), nseg.value
+
+
+def centroids(xyz, nv):
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    nel = xyz.shape[0]
+    out = np.zeros((nel, 3), np.float64)
+    lib().oracle_centroids(_p(out), _p(xyz), nel, nv)
+    return out
+
+
+def tree_sum(x):
+    x = np.ascontiguousarray(x, np.float64)
+    return lib().oracle_tree_sum(_p(x), len(x))
+
+
+def power_serial(A, N):
+    A = np.ascontiguousarray(A, np.float64).ravel()
+    y = np.zeros(3, np.float64)
+    it = lib().oracle_power_serial(_p(y), N, _p(A))
+    return y[:N], it
+
+
+def tqli(diag, upper):
+    n = len(diag)
+    diag = np.ascontiguousarray(diag, np.float64)
+    upper = np.ascontiguousarray(np.concatenate([upper, [0.0]])[:max(n, 1)],
+                                 np.float64)
+    ev = np.zeros((n, n), np.float64)
+    ew = np.zeros(n, np.float64)
+    rc = lib().oracle_tqli(_p(ev), _p(ew), n, _p(diag), _p(upper))
+    return rc, ew, ev
+
+
+def laplacian(x, vtx):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.zeros_like(x)
+    lib().oracle_laplacian(_p(y), _p(x), _p(vtx), len(vtx), vtx.shape[1])
+    return y
+
+
+def dual_graph(vtx):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    nel, nv = vtx.shape
+    cap = nel * 64 + 16
+    rowptr = np.zeros(nel + 1, np.int64)
+    col = np.zeros(cap, np.int32)
+    w = np.zeros(cap, np.int32)
+    nnz = lib().oracle_dual_graph(_p(rowptr), _p(col), _p(w), cap, _p(vtx),
+                                  nel, nv)
+    assert nnz >= 0
+    return rowptr, col[:nnz].copy(), w[:nnz].copy()
+
+
+def components(vtx, mask=None):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    m = None if mask is None else np.ascontiguousarray(mask, np.int32)
+    return lib().oracle_components(_p(vtx), _p(m), len(vtx), vtx.shape[1])
+
+
+def part_quality(part, vtx, nparts):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    part = np.ascontiguousarray(part, np.int32)
+    q = np.zeros(8, np.float64)
+    lib().oracle_part_quality(_p(q), _p(part), _p(vtx), len(vtx),
+                              vtx.shape[1], nparts)
+    return q
+
+
+def fiedler(vtx, miter=50, mpass=50, tol=1e-5):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    f = np.zeros(len(vtx), np.float64)
+    it = lib().oracle_fiedler(_p(f), _p(vtx), len(vtx), vtx.shape[1], miter,
+                              mpass, tol)
+    return f, it

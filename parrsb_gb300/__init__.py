@@ -1,0 +1,183 @@
+"""parrsb_gb300 -- GB300 (sm_103a) implementation of parRSB's partitioning
+(RSB / RCB / RIB) and connectivity (gencon) path behind a drop-in C ABI.
+
+The compute path is the in-tree CUDA library ``libparrsb_gb300.so`` (built by
+``parrsb_gb300.build``).  This module binds its C ABI with ctypes and mirrors
+the reference entry points:
+
+* ``part_mesh(vtx, xyz, nparts, **options)`` -- parrsb_part_mesh
+  (src/parRSB.h:45-48) with an explicit part count instead of MPI_Comm.
+* ``conn_mesh(coord, ndim, tol)`` -- parrsb_conn_mesh (src/parRSB.h:62-64).
+
+There is no CPU fallback: importing works without a GPU (so option handling
+and argument checks can be tested), but any call that reaches the GPU raises
+``ParrsbError`` when the library or the device is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .options import (ERR_ARGS, ERR_CHECK, ERR_CUDA, ERR_UNSUPPORTED, OK,
+                      ParrsbOptions, DEFAULTS)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libparrsb_gb300.so")
+
+# Exported symbols declared in include/parrsb.h
+EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
+           "fparrsb_conn_mesh", "parrsb_part_mesh_device",
+           "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
+           "parrsb_gpu_finalize"]
+
+
+class ParrsbError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__(f"{what} failed with code {code}")
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_double),
+                ("stage_ms", ctypes.c_double * 12),
+                ("lanczos_iters", ctypes.c_longlong),
+                ("lanczos_row_iters", ctypes.c_longlong),
+                ("spmv_launches", ctypes.c_longlong),
+                ("spmv_ms", ctypes.c_double),
+                ("spmv_bytes", ctypes.c_longlong),
+                ("kernel_launches", ctypes.c_longlong),
+                ("levels", ctypes.c_int),
+                ("max_components", ctypes.c_int),
+                ("max_fiedler_resid", ctypes.c_double),
+                ("unconverged", ctypes.c_int),
+                ("nnz", ctypes.c_longlong),
+                ("gencon_segments", ctypes.c_longlong)]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if name == "stage_ms" else v
+        return d
+
+
+STAGES = ["upload", "setup", "pre", "lanczos", "tqli", "sort", "components",
+          "balance", "restrict", "download", "gencon", "check"]
+
+_lib = None
+
+
+def library(build_if_missing=False):
+    """Load the CUDA library (raises if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from .build import build
+            build()
+        else:
+            raise ParrsbError(ERR_CUDA, f"CUDA library not built ({LIB_PATH})")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    L.parrsb_part_mesh.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(ParrsbOptions), ctypes.c_int]
+    L.parrsb_part_mesh.restype = ctypes.c_int
+    L.parrsb_part_mesh_device.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ParrsbOptions),
+                                          ctypes.c_int]
+    L.parrsb_conn_mesh.argtypes = [P, P, ctypes.c_uint, ctypes.c_uint, P,
+                                   ctypes.c_int, ctypes.c_double]
+    L.parrsb_conn_mesh.restype = ctypes.c_int
+    L.parrsb_conn_mesh_device.argtypes = [P, P, ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.c_double]
+    L.fparrsb_conn_mesh.argtypes = [P, P, P, P, P, P, P, P]
+    L.fparrsb_conn_mesh.restype = None
+    L.parrsb_get_stats.argtypes = [ctypes.POINTER(Stats)]
+    L.parrsb_part_quality.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_int]
+    L.parrsb_gpu_finalize.argtypes = []
+    L.parrsb_gpu_finalize.restype = None
+    _lib = L
+    return L
+
+
+def default_options():
+    """Copy of the library's exported parrsb_default_options."""
+    o = ParrsbOptions.in_dll(library(), "parrsb_default_options")
+    return ParrsbOptions(**o.as_dict())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def part_mesh(vtx, xyz, nparts, options=None, tag=None, **kw):
+    """Partition elements into `nparts` parts (parrsb_part_mesh).
+
+    vtx: (nel, nv) int64 vertex ids or None; xyz: (nel, nv, ndim) float64
+    corner coordinates or None.  Options may be a ParrsbOptions (mutated in
+    place with environment overrides, as the reference does) or keywords.
+    Returns part (nel,) int32.  Raises ParrsbError on a nonzero return."""
+    if options is None:
+        kw.setdefault("verbose_level", 0)
+        options = ParrsbOptions.make(**kw)
+    nel = len(vtx) if vtx is not None else len(xyz)
+    nv = vtx.shape[1] if vtx is not None else xyz.shape[1]
+    vtx = None if vtx is None else np.ascontiguousarray(vtx, np.int64)
+    xyz = None if xyz is None else np.ascontiguousarray(xyz, np.float64)
+    tag = None if tag is None else np.ascontiguousarray(tag, np.int32)
+    part = np.full(nel, -1, np.int32)
+    rc = library().parrsb_part_mesh(_ptr(part), _ptr(vtx), _ptr(xyz), _ptr(tag),
+                                    nel, nv, ctypes.byref(options), nparts)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_part_mesh")
+    return part
+
+
+def conn_mesh(coord, ndim, tol=0.2, periodic=None):
+    """Vertex ids from corner coordinates (parrsb_conn_mesh).  coord:
+    (nel, nv, ndim) in Nek preprocessor corner order.  Returns (nel, nv)
+    int64 ids in symmetric corner order.  Raises ParrsbError (code 1 when
+    the element or face check fails)."""
+    coord = np.ascontiguousarray(coord, np.float64)
+    nv = 4 if ndim == 2 else 8
+    nel = coord.size // (nv * ndim)
+    vtx = np.zeros(nel * nv, np.int64)
+    npf = 0 if periodic is None else len(periodic)
+    pinfo = None if periodic is None else np.ascontiguousarray(periodic, np.int64)
+    rc = library().parrsb_conn_mesh(_ptr(vtx), _ptr(coord), nel, ndim,
+                                    _ptr(pinfo), npf, tol)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_conn_mesh")
+    return vtx.reshape(nel, nv)
+
+
+def part_quality(part, vtx, nparts):
+    """Quality figures of a partition, computed on the GPU (see
+    include/parrsb.h parrsb_part_quality)."""
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    part = np.ascontiguousarray(part, np.int32)
+    q = np.zeros(8, np.float64)
+    rc = library().parrsb_part_quality(_ptr(q), _ptr(part), _ptr(vtx), len(vtx),
+                                       vtx.shape[1], nparts)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_part_quality")
+    return q
+
+
+def last_stats():
+    s = Stats()
+    library().parrsb_get_stats(ctypes.byref(s))
+    return s
+
+
+def finalize():
+    if _lib is not None:
+        _lib.parrsb_gpu_finalize()
+
+
+__all__ = ["part_mesh", "conn_mesh", "part_quality", "last_stats",
+           "default_options", "ParrsbOptions", "ParrsbError", "DEFAULTS",
+           "library", "finalize", "OK", "ERR_ARGS", "ERR_CUDA", "ERR_CHECK",
+           "ERR_UNSUPPORTED"]

@@ -1,0 +1,38 @@
+// bisect.cuh -- centroids and the segmented coordinate / inertial bisection
+// engine (RCB, RIB and their rank-local recursions).
+#pragma once
+#include "sort.cuh"
+#include "util.cuh"
+
+namespace prsb {
+
+// cent[d*N + e] = centroid coordinate d of element e (d < 3; 0 for 2D z):
+// sequential sum over the nv corners, then a division by nv.
+void compute_centroids(const double *xyz, int nel, int nv, double *cent);
+
+enum BisectKind { BISECT_RCB = 0, BISECT_RIB = 1 };
+
+struct BisectWs {
+  SortWs sort;
+  DBuf<u64> keys;
+  DBuf<int> vals;
+  DBuf<int> seg_of_pos, seg_of_elem, axis;
+  DBuf<double> red_a, red_b, ev;   // reduction partials, eigenvectors
+  DBuf<ll> tile_off, child_off;
+  DBuf<int> child_cnt;
+  SegTable t2;
+};
+
+// Recursive bisection of every segment of `t` (segments tile [0, N) of the
+// order `perm`).  A segment with p > 1 virtual ranks is split at
+// lower_count(n, p) after a stable sort along its axis (RCB: longest
+// bounding-box edge; RIB: dominant inertia eigenvector).  With do_local, a
+// segment with p == 1 is then recursively halved at n/2 the same way
+// (rcb_local / rib_local), which only reorders it.  On return `perm` holds
+// the final order and, if part_of_elem is not null, part_of_elem[e] is the
+// rank (r0 of the final segment) of element e.
+void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
+                     const double *cent, ll N, int ndim, bool do_local,
+                     int *part_of_elem, BisectWs &ws);
+
+}  // namespace prsb

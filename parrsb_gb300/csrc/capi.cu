@@ -1,0 +1,433 @@
+// capi.cu -- the drop-in C ABI (include/parrsb.h).
+//
+// parrsb_part_mesh restates parrsb_part_mesh / parrsb_part_mesh_v0
+// (src/parrsb.c:236-290, 853-906) with `nparts` virtual ranks instead of an
+// MPI communicator; parrsb_conn_mesh restates src/con.c:189-295 on one rank.
+// Option handling (defaults, PARRSB_* environment overrides written back into
+// the caller's struct, levels clamped to 2, rsb_pre = 0 without coordinates)
+// follows src/parrsb.c:26-77, 229, 250.  Errors are returned, never exit().
+#include <stdarg.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <chrono>
+#include <stdexcept>
+
+#include "bisect.cuh"
+#include "gencon.cuh"
+#include "rsb.cuh"
+
+extern "C" {
+parrsb_options parrsb_default_options = {
+    /*partitioner*/ 0, /*tagged*/ 0, /*levels*/ 2, /*find_disconnected_comps*/ 1,
+    /*repair*/ 0, /*verbose_level*/ 1, /*profile_level*/ 0, /*rsb_algo*/ 0,
+    /*rsb_pre*/ 1, /*rsb_max_iter*/ 50, /*rsb_max_passes*/ 50, /*rsb_tol*/ 1e-5,
+    /*rsb_dump_stats*/ 0, /*rsb_mg_grammian*/ 0, /*rsb_mg_factor*/ 2};
+}
+
+namespace prsb {
+
+static thread_local Ctx g_ctx;
+Ctx &ctx() { return g_ctx; }
+
+void Ctx::init() {
+  if (!stream) CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  memset(&stats, 0, sizeof(stats));
+  kernel_launches = 0;
+  const char *t = getenv("PARRSB_GPU_TIMING");
+  timing = t && atoi(t) != 0;
+}
+
+namespace {
+
+struct Workspace {
+  GenconWs gc;
+  DBuf<long long> vtx;
+  DBuf<double> xyz, cent;
+  DBuf<int> part;
+  DBuf<long long> ids;
+};
+thread_local Workspace *g_ws = nullptr;
+Workspace &ws() {
+  if (!g_ws) g_ws = new Workspace();
+  return *g_ws;
+}
+
+void print_if(int verbose, const char *fmt, ...) {
+  if (verbose <= 0) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vprintf(fmt, ap);
+  va_end(ap);
+  printf("\n");
+  fflush(stdout);
+}
+
+void update_options(parrsb_options *o) {
+#define UPD(F, S, INT)                     \
+  do {                                     \
+    const char *v = getenv(S);             \
+    if (v) {                               \
+      if (INT)                             \
+        o->F = atoi(v);                    \
+      else                                 \
+        o->F = atof(v);                    \
+    }                                      \
+  } while (0)
+  UPD(partitioner, "PARRSB_PARTITIONER", 1);
+  UPD(tagged, "PARRSB_TAGGED", 1);
+  UPD(levels, "PARRSB_LEVELS", 1);
+  UPD(find_disconnected_comps, "PARRSB_FIND_DISCONNECTED_COMPONENTS", 1);
+  UPD(repair, "PARRSB_REPAIR", 1);
+  UPD(verbose_level, "PARRSB_VERBOSE_LEVEL", 1);
+  UPD(profile_level, "PARRSB_PROFILE_LEVEL", 1);
+  UPD(rsb_algo, "PARRSB_RSB_ALGO", 1);
+  UPD(rsb_pre, "PARRSB_RSB_PRE", 1);
+  UPD(rsb_max_iter, "PARRSB_RSB_MAX_ITER", 1);
+  UPD(rsb_max_passes, "PARRSB_RSB_MAX_PASSES", 1);
+  UPD(rsb_tol, "PARRSB_RSB_TOL", 0);
+  UPD(rsb_mg_grammian, "PARRSB_RSB_MG_GRAMMIAN", 1);
+  UPD(rsb_mg_factor, "PARRSB_RSB_MG_FACTOR", 1);
+#undef UPD
+}
+
+void print_options(const parrsb_options *o) {
+  int v = o->verbose_level;
+  print_if(v, "PARRSB_PARTITIONER = %d", o->partitioner);
+  print_if(v, "PARRSB_TAGGED = %d", o->tagged);
+  print_if(v, "PARRSB_LEVELS = %d", o->levels);
+  print_if(v, "PARRSB_FIND_DISCONNECTED_COMPONENTS = %d", o->find_disconnected_comps);
+  print_if(v, "PARRSB_REPAIR = %d", o->repair);
+  print_if(v, "PARRSB_VERBOSE_LEVEL = %d", o->verbose_level);
+  print_if(v, "PARRSB_PROFILE_LEVEL = %d", o->profile_level);
+  print_if(v, "PARRSB_RSB_ALGO = %d", o->rsb_algo);
+  print_if(v, "PARRSB_RSB_PRE = %d", o->rsb_pre);
+  print_if(v, "PARRSB_RSB_MAX_ITER = %d", o->rsb_max_iter);
+  print_if(v, "PARRSB_RSB_MAX_PASSES = %d", o->rsb_max_passes);
+  print_if(v, "PARRSB_RSB_TOL = %lf", o->rsb_tol);
+  print_if(v, "PARRSB_RSB_MG_GRAMMIAN = %d", o->rsb_mg_grammian);
+  print_if(v, "PARRSB_RSB_MG_FACTOR = %d", o->rsb_mg_factor);
+}
+
+int env_int(const char *name, int def) {
+  const char *v = getenv(name);
+  return v ? atoi(v) : def;
+}
+
+// Validates and normalises options (shared by the host and device entries).
+int prepare_options(const long long *vtx, const double *xyz, int nel, int nv,
+                    parrsb_options *o, int nparts, const int *tag, bool print) {
+  if (!o) return PARRSB_ERR_ARGS;
+  update_options(o);
+  if (print) {
+    print_if(o->verbose_level, "Running parRSB ..., nv = %d, nelg = %lld", nv, (long long)nel);
+    print_options(o);
+  }
+  if (o->tagged == 1 && !tag) {
+    print_if(o->verbose_level, "Tagged partitioning requested but tag array is NULL..");
+    return PARRSB_ERR_ARGS;
+  }
+  if (o->tagged == 1) return PARRSB_ERR_UNSUPPORTED;
+  if (nel < 0 || nparts < 1 || nv < 1 || nv > 8) return PARRSB_ERR_ARGS;
+  if (vtx == nullptr && xyz == nullptr) {
+    print_if(o->verbose_level,
+             "parrsb_part_mesh_v0: Both vertices and coordinates can't be NULL");
+    return PARRSB_ERR_ARGS;
+  }
+  if (xyz == nullptr) o->rsb_pre = 0;
+  if (o->levels > 2) o->levels = 2;
+  if (o->partitioner == 0) {
+    if (o->rsb_algo != 0) return PARRSB_ERR_UNSUPPORTED;
+    if (vtx == nullptr) return PARRSB_ERR_ARGS;
+  }
+  return PARRSB_OK;
+}
+
+__global__ void k_block_part(int *part, ll nel, int nparts) {
+  ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  ll nstar = nel / nparts, nrem = nel - nstar * nparts, lower = (nstar + 1) * nrem;
+  ll eg = e + 1;
+  int p;
+  if (nstar == 0)
+    p = (int)(eg - 1);
+  else if (eg <= lower)
+    p = (int)((eg - 1) / (nstar + 1));
+  else
+    p = (int)((eg - 1 - lower) / nstar + nrem);
+  part[e] = p;
+}
+
+// Device-resident partitioning: inputs and output already in HBM.
+void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int nel, int nv,
+                   const parrsb_options *o, int nparts) {
+  cudaStream_t st = ctx().stream;
+  if (nel == 0) return;
+  int ndim = (nv == 8) ? 3 : 2;
+  ll N = nel;
+  int P = nparts < nel ? nparts : nel;
+  Workspace &W = ws();
+  W.cent.ensure((size_t)3 * N);
+  {
+    StageTimer tm(PARRSB_STAGE_SETUP);
+    compute_centroids(d_xyz, nel, nv, W.cent.p);
+  }
+  if (o->partitioner == 1 || o->partitioner == 2) {
+    StageTimer tm(PARRSB_STAGE_PRE);
+    BisectWs bws;
+    DBuf<int> perm((size_t)N);
+    std::vector<int> h(N);
+    for (ll i = 0; i < N; i++) h[i] = (int)i;
+    h2d(perm.p, h.data(), N);
+    SegTable t;
+    t.reserve(1);
+    ll s0 = 0, n0 = N;
+    int p0 = P, r00 = 0;
+    h2d(t.start.p, &s0, 1);
+    h2d(t.n.p, &n0, 1);
+    h2d(t.p.p, &p0, 1);
+    h2d(t.r0.p, &r00, 1);
+    t.count = 1;
+    bisect_segments(o->partitioner == 1 ? BISECT_RCB : BISECT_RIB, perm, t, W.cent.p, N, ndim,
+                    false, d_part, bws);
+    sync();
+  } else if (o->partitioner == 0) {
+    RsbOpts ro;
+    ro.pre = o->rsb_pre;
+    ro.miter = o->rsb_max_iter;
+    ro.mpass = o->rsb_max_passes;
+    ro.tol = o->rsb_tol;
+    ro.find_comps = o->find_disconnected_comps;
+    ro.profile = o->profile_level;
+    ro.fp32 = env_int("PARRSB_GPU_FP32", 0);
+    ro.check_resid = env_int("PARRSB_GPU_CHECK_RESID", 1);
+    ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
+    rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part);
+    sync();
+  } else {
+    k_block_part<<<grid_for(N, 256), 256, 0, st>>>(d_part, N, nparts);
+    CK_LAUNCH();
+    sync();
+  }
+}
+
+const char *stage_names[12] = {"upload", "setup", "pre-partition", "lanczos",
+                               "tqli+ritz", "sort", "components", "balance",
+                               "restrict", "download", "gencon", "check"};
+
+void print_profile(const parrsb_options *o) {
+  if (o->profile_level <= 0) return;
+  const parrsb_stats &S = ctx().stats;
+  for (int i = 0; i < 12; i++)
+    if (S.stage_ms[i] > 0) printf("  %-14s %10.3f ms\n", stage_names[i], S.stage_ms[i]);
+  printf("  lanczos steps %lld, levels %d, max components %d, max residual %.3e\n",
+         S.lanczos_iters, S.levels, S.max_components, S.max_fiedler_resid);
+  fflush(stdout);
+}
+
+template <typename F>
+int guarded(F &&fn) {
+  try {
+    return fn();
+  } catch (const CudaError &e) {
+    fprintf(stderr, "parrsb_gb300: CUDA error %s at %s:%d\n", cudaGetErrorString(e.err), e.file,
+            e.line);
+    cudaGetLastError();
+    return PARRSB_ERR_CUDA;
+  } catch (const ArgError &e) {
+    fprintf(stderr, "parrsb_gb300: %s\n", e.msg);
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    fprintf(stderr, "parrsb_gb300: host allocation failed\n");
+    return PARRSB_ERR_CUDA;
+  }
+}
+
+// Host-side fault injection for tests: PARRSB_FAULT=<stage> makes that stage
+// fail with PARRSB_ERR_CHECK after everything before it ran.
+void maybe_fault(const char *stage) {
+  const char *f = getenv("PARRSB_FAULT");
+  if (f && strcmp(f, stage) == 0) throw ArgError{PARRSB_ERR_CHECK, "injected fault"};
+}
+
+}  // namespace
+}  // namespace prsb
+
+using namespace prsb;
+
+extern "C" int parrsb_part_mesh(int *part, const long long *vtx, const double *xyz,
+                                const int *tag, int nel, int nv, parrsb_options *options,
+                                int nparts) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = prepare_options(vtx, xyz, nel, nv, options, nparts, tag, true);
+  if (rc != PARRSB_OK) return rc;
+  if (nel > 0 && !part) return PARRSB_ERR_ARGS;
+  rc = guarded([&]() -> int {
+    ctx().init();
+    Workspace &W = ws();
+    ll N = nel;
+    if (N == 0) return PARRSB_OK;
+    int ndim = (nv == 8) ? 3 : 2;
+    {
+      StageTimer tm(PARRSB_STAGE_UPLOAD);
+      if (vtx) {
+        W.vtx.ensure((size_t)N * nv);
+        h2d(W.vtx.p, vtx, (size_t)N * nv);
+      }
+      if (xyz) {
+        W.xyz.ensure((size_t)N * nv * ndim);
+        h2d(W.xyz.p, xyz, (size_t)N * nv * ndim);
+      }
+      W.part.ensure((size_t)N);
+    }
+    maybe_fault("upload");
+    part_mesh_dev(W.part.p, vtx ? W.vtx.p : nullptr, xyz ? W.xyz.p : nullptr, nel, nv, options,
+                  nparts);
+    maybe_fault("partition");
+    {
+      StageTimer tm(PARRSB_STAGE_DOWNLOAD);
+      d2h(part, W.part.p, (size_t)N);
+    }
+    sync();
+    return PARRSB_OK;
+  });
+  double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx().stats.total_ms = sec * 1e3;
+  ctx().stats.kernel_launches = ctx().kernel_launches;
+  static const char *ALGO[3] = {"RSB", "RCB", "RIB"};
+  if (rc == PARRSB_OK) {
+    int pa = options->partitioner;
+    print_if(options->verbose_level, "par%s finished in %g seconds.",
+             (pa >= 0 && pa < 3) ? ALGO[pa] : "RSB", sec);
+    print_profile(options);
+  }
+  return rc;
+}
+
+extern "C" int parrsb_part_mesh_device(int *d_part, const long long *d_vtx, const double *d_xyz,
+                                       int nel, int nv, parrsb_options *options, int nparts) {
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = prepare_options(d_vtx, d_xyz, nel, nv, options, nparts, nullptr, false);
+  if (rc != PARRSB_OK) return rc;
+  rc = guarded([&]() -> int {
+    ctx().init();
+    part_mesh_dev(d_part, d_vtx, d_xyz, nel, nv, options, nparts);
+    return PARRSB_OK;
+  });
+  ctx().stats.total_ms =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() * 1e3;
+  ctx().stats.kernel_launches = ctx().kernel_launches;
+  return rc;
+}
+
+extern "C" int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel, unsigned nDim,
+                                long long *periodicInfo, int nPeriodicFaces, double tol) {
+  (void)periodicInfo;
+  int verbose = 1;
+  if (const char *v = getenv("PARRSB_VERBOSE_LEVEL")) verbose = atoi(v);
+  if (nDim < 2 || nDim > 3) return PARRSB_ERR_ARGS;
+  if (nPeriodicFaces > 0) return PARRSB_ERR_UNSUPPORTED;
+  if (nel > 0 && (!vtx || !coord)) return PARRSB_ERR_ARGS;
+  auto t0 = std::chrono::steady_clock::now();
+  print_if(verbose, "Running parCon ...");
+  int rc = guarded([&]() -> int {
+    ctx().init();
+    Workspace &W = ws();
+    int nv = nDim == 2 ? 4 : 8;
+    ll np = (ll)nel * nv;
+    if (np == 0) return PARRSB_OK;
+    {
+      StageTimer tm(PARRSB_STAGE_UPLOAD);
+      W.xyz.ensure((size_t)np * nDim);
+      h2d(W.xyz.p, coord, (size_t)np * nDim);
+      W.ids.ensure((size_t)np);
+    }
+    ll nseg = 0;
+    int r;
+    {
+      StageTimer tm(PARRSB_STAGE_GENCON);
+      r = gencon_device(W.ids.p, W.xyz.p, nel, (int)nDim, tol, W.gc, &nseg, nullptr);
+    }
+    ctx().stats.gencon_segments = nseg;
+    if (r != PARRSB_OK) {
+      print_if(1, "\t%s:%d element_check / face_check failed.", __FILE__, __LINE__);
+      return r;
+    }
+    {
+      StageTimer tm(PARRSB_STAGE_DOWNLOAD);
+      d2h(vtx, W.ids.p, (size_t)np);
+      sync();
+    }
+    return PARRSB_OK;
+  });
+  double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx().stats.total_ms = sec * 1e3;
+  ctx().stats.kernel_launches = ctx().kernel_launches;
+  if (rc == PARRSB_OK) print_if(verbose, "parCon (tol = %e) finished in %g s", tol, sec);
+  return rc;
+}
+
+extern "C" int parrsb_conn_mesh_device(long long *d_vtx, const double *d_coord, unsigned int nel,
+                                       unsigned nDim, double tol) {
+  if (nDim < 2 || nDim > 3) return PARRSB_ERR_ARGS;
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = guarded([&]() -> int {
+    ctx().init();
+    ll nseg = 0;
+    int r = gencon_device(d_vtx, d_coord, nel, (int)nDim, tol, ws().gc, &nseg, nullptr);
+    ctx().stats.gencon_segments = nseg;
+    sync();
+    return r;
+  });
+  ctx().stats.total_ms =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() * 1e3;
+  ctx().stats.kernel_launches = ctx().kernel_launches;
+  return rc;
+}
+
+extern "C" void fparrsb_conn_mesh(long long *vtx, double *coord, int *nel, int *nDim,
+                                  long long *periodicInfo, int *nPeriodicFaces, double *tol,
+                                  int *err) {
+  *err = 1;
+  *err = parrsb_conn_mesh(vtx, coord, (unsigned)*nel, (unsigned)*nDim, periodicInfo,
+                          *nPeriodicFaces, *tol);
+}
+
+extern "C" int parrsb_get_stats(parrsb_stats *out) {
+  if (!out) return PARRSB_ERR_ARGS;
+  *out = ctx().stats;
+  return PARRSB_OK;
+}
+
+extern "C" int parrsb_part_quality(double *q, const int *part, const long long *vtx, int nel,
+                                   int nv, int nparts) {
+  if (!q || nel < 0 || nparts < 1 || nv < 1 || nv > 8) return PARRSB_ERR_ARGS;
+  if (nel > 0 && (!part || !vtx)) return PARRSB_ERR_ARGS;
+  for (int i = 0; i < nel; i++)
+    if (part[i] < 0 || part[i] >= nparts) return PARRSB_ERR_ARGS;
+  return guarded([&]() -> int {
+    ctx().init();
+    ll N = nel;
+    if (N == 0) {
+      for (int i = 0; i < 8; i++) q[i] = 0.0;
+      return PARRSB_OK;
+    }
+    DBuf<long long> dv((size_t)N * nv);
+    DBuf<int> dp((size_t)N);
+    h2d(dv.p, vtx, (size_t)N * nv);
+    h2d(dp.p, part, (size_t)N);
+    part_quality_device(dv.p, dp.p, N, nv, nparts, q);
+    return PARRSB_OK;
+  });
+}
+
+extern "C" void parrsb_gpu_finalize(void) {
+  if (g_ws) {
+    delete g_ws;
+    g_ws = nullptr;
+  }
+  if (g_ctx.stream) {
+    cudaStreamDestroy(g_ctx.stream);
+    g_ctx.stream = nullptr;
+  }
+}

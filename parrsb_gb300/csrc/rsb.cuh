@@ -1,0 +1,49 @@
+// rsb.cuh -- recursive spectral bisection on one GPU.
+#pragma once
+#include "bisect.cuh"
+
+namespace prsb {
+
+// Element dual graph in original element order (CSR).  Weight of (a, b) =
+// number of (corner of a, corner of b) pairs with the same vertex id.
+struct Graph {
+  DBuf<ll> rowptr;
+  DBuf<int> col;
+  DBuf<unsigned char> w;
+  ll n = 0, nnz = 0;
+  int max_row = 0, max_w = 0;
+};
+
+void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g,
+                      SortWs &sws);
+
+struct RsbOpts {
+  int pre = 1;          // 0 none, 1 RCB, 2 RIB
+  int miter = 50;
+  int mpass = 50;
+  double tol = 1e-5;
+  int find_comps = 1;
+  int fp32 = 0;         // FP32 Lanczos vectors (FP64 dots / T / eigensolve)
+  int check_resid = 1;  // FP64 eigen-residual of every Fiedler vector
+  int profile = 0;
+  int use_graphs = 1;   // capture each Lanczos pass in a CUDA graph
+};
+
+// Partition N elements (vertex ids d_vtx, centroids cent) into P parts.
+void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv,
+                int P, const RsbOpts &o, int *d_part);
+
+// Fiedler vectors of independent element groups: group g is the elements
+// e with group_of[e] == g (groups listed in element order).  Used by the
+// batched level solve; f receives the normalised Fiedler vector per element
+// and iters (host, ngroups) the Lanczos steps of each group.
+void fiedler_groups_device(const long long *d_vtx, ll N, int nv,
+                           const int *d_group_of, int ngroups,
+                           const RsbOpts &o, double *d_f, long long *iters,
+                           double *resid);
+
+// Quality of a partition (see parrsb_part_quality).
+void part_quality_device(const long long *d_vtx, const int *d_part, ll N,
+                         int nv, int nparts, double *q);
+
+}  // namespace prsb

@@ -1,0 +1,172 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle.
+
+Bar: RCB / RIB parts and orders, gencon ids, component counts and quality
+figures are bit-exact; RSB partitions have the same part sizes and an edge
+cut within 1% of the oracle's partition of the same input (FP64 and FP32
+Lanczos vectors), with the FP64-checked Fiedler residual reported.
+"""
+import numpy as np
+import pytest
+
+import parrsb_gb300 as P
+from parrsb_gb300 import meshgen
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu(lib):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    yield
+    P.finalize()
+
+
+# ---------------------------------------------------------------- RCB / RIB
+@pytest.mark.parametrize("partitioner", [1, 2])
+@pytest.mark.parametrize("shape,nparts", [((16, 16, 16), 8), ((16, 16, 16), 7),
+                                          ((12, 9, 5), 100), ((5, 4, 3), 64),
+                                          ((3, 1, 1), 2), ((1, 1, 1), 4)])
+def test_bisection_3d_bit_exact(oracle, partitioner, shape, nparts):
+    vtx, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=sum(shape) + nparts)
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=partitioner)
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, nparts, partitioner=partitioner)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
+
+
+@pytest.mark.parametrize("partitioner", [1, 2])
+@pytest.mark.parametrize("nparts", [1, 3, 1024])
+def test_bisection_annulus_bit_exact(oracle, partitioner, nparts):
+    vtx, xyz = meshgen.annulus_quad(128, 64, amp=0.02, seed=7)
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=partitioner)
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, nparts, partitioner=partitioner)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
+
+
+def test_rcb_without_vertices(oracle):
+    _, xyz = meshgen.box_hex(10, 6, 4, jitter=0.1, seed=1)
+    part = P.part_mesh(None, xyz, 12, partitioner=1)
+    rc, ref, _, _, _ = oracle.part_mesh(None, xyz, 12, partitioner=1)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
+
+
+def test_unknown_partitioner_block_distribution(oracle):
+    vtx, xyz = meshgen.box_hex(5, 5, 3, jitter=0.0, seed=0)
+    part = P.part_mesh(vtx, xyz, 7, partitioner=9)
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, 7, partitioner=9)
+    np.testing.assert_array_equal(part, ref)
+
+
+# ------------------------------------------------------------------ gencon
+@pytest.mark.parametrize("shape", [(16, 16, 16), (7, 5, 3), (1, 1, 1)])
+def test_gencon_box_bit_exact(oracle, shape):
+    _, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=11)
+    ids = P.conn_mesh(xyz, 3, 0.2)
+    rc, ref, _, nseg = oracle.conn_mesh(xyz, 3, 0.2)
+    assert rc == 0
+    np.testing.assert_array_equal(ids, ref)
+    assert P.last_stats().gencon_segments == nseg
+
+
+def test_gencon_annulus_small_bit_exact(oracle):
+    _, xyz = meshgen.annulus_quad(64, 64, amp=0.02, seed=0)
+    ids = P.conn_mesh(xyz, 2, 0.2)
+    rc, ref, _, nseg = oracle.conn_mesh(xyz, 2, 0.2)
+    assert rc == 0 and nseg == 64 * 65
+    np.testing.assert_array_equal(ids, ref)
+
+
+def test_gencon_annulus_512_fails_like_reference(oracle):
+    """The sort-and-gap matcher cannot separate the vertices of the dense
+    512x512 annulus at tol 0.2: element_check fails in the oracle and the
+    GPU returns the same error code with the same number of segments."""
+    _, xyz = meshgen.annulus_quad(512, 512, amp=0.02, seed=0)
+    rc, _, _, nseg = oracle.conn_mesh(xyz, 2, 0.2)
+    assert rc == 1
+    with pytest.raises(P.ParrsbError) as ei:
+        P.conn_mesh(xyz, 2, 0.2)
+    assert ei.value.code == 1
+    assert P.last_stats().gencon_segments == nseg
+
+
+def test_gencon_pipe_bit_exact(oracle):
+    _, xyz = meshgen.pipe_hex(24, 6, 5, jitter=0.05, seed=2)
+    ids = P.conn_mesh(xyz, 3, 0.2)
+    rc, ref, _, _ = oracle.conn_mesh(xyz, 3, 0.2)
+    assert rc == 0
+    np.testing.assert_array_equal(ids, ref)
+
+
+# ------------------------------------------------------------------ quality
+def test_quality_matches_oracle(oracle):
+    vtx, xyz = meshgen.box_hex(12, 10, 8, jitter=0.1, seed=4)
+    rc, part, _, _, _ = oracle.part_mesh(vtx, xyz, 9, partitioner=1)
+    q = P.part_quality(part, vtx, 9)
+    qr = oracle.part_quality(part, vtx, 9)
+    np.testing.assert_array_equal(q, qr)
+
+
+# --------------------------------------------------------------------- RSB
+def _rsb_compare(oracle, vtx, xyz, nparts, tol_cut=0.01, **opts):
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=0, **opts)
+    st = P.last_stats()
+    rc, ref, _, info, _ = oracle.part_mesh(vtx, xyz, nparts, partitioner=0, **opts)
+    assert rc == 0
+    sizes = np.bincount(part, minlength=nparts)
+    ref_sizes = np.bincount(ref, minlength=nparts)
+    q = oracle.part_quality(part, vtx, nparts)
+    qr = oracle.part_quality(ref, vtx, nparts)
+    return part, ref, sizes, ref_sizes, q, qr, st, info
+
+
+def test_rsb_box_16_fp64(oracle):
+    vtx, xyz = meshgen.box_hex(16, 16, 16, jitter=0.1, seed=0)
+    part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, 8)
+    np.testing.assert_array_equal(sizes, rs)
+    assert q[0] <= qr[0] * 1.01 and q[0] >= qr[0] * 0.99
+    assert st.max_fiedler_resid < 1e-3
+    assert st.levels == 3
+
+
+@pytest.mark.parametrize("nparts", [3, 5, 7])
+def test_rsb_uneven_balance(oracle, nparts):
+    vtx, xyz = meshgen.box_hex(10, 9, 7, jitter=0.1, seed=nparts)
+    part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, nparts)
+    np.testing.assert_array_equal(np.sort(sizes), np.sort(rs))
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0] + 1e-9
+
+
+def test_rsb_fp32_vectors(oracle, monkeypatch):
+    monkeypatch.setenv("PARRSB_GPU_FP32", "1")
+    vtx, xyz = meshgen.box_hex(16, 16, 8, jitter=0.1, seed=5)
+    part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, 8)
+    np.testing.assert_array_equal(sizes, rs)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+
+
+def test_rsb_no_graphs_same_result(oracle, monkeypatch):
+    vtx, xyz = meshgen.box_hex(12, 8, 6, jitter=0.1, seed=9)
+    a = P.part_mesh(vtx, xyz, 4, partitioner=0)
+    monkeypatch.setenv("PARRSB_GPU_GRAPHS", "0")
+    b = P.part_mesh(vtx, xyz, 4, partitioner=0)
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("pre", [0, 2])
+def test_rsb_other_prepartitioners(oracle, pre):
+    vtx, xyz = meshgen.box_hex(12, 10, 6, jitter=0.1, seed=pre)
+    part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, 4, rsb_pre=pre)
+    np.testing.assert_array_equal(sizes, rs)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+
+
+def test_rsb_repeatable(oracle):
+    vtx, xyz = meshgen.box_hex(10, 10, 10, jitter=0.1, seed=1)
+    a = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    b = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    np.testing.assert_array_equal(a, b)
