@@ -30,8 +30,24 @@ namespace prsb {
 static thread_local Ctx g_ctx;
 Ctx &ctx() { return g_ctx; }
 
+void *dev_alloc(size_t bytes) {
+  void *p = nullptr;
+  CK(cudaMallocAsync(&p, bytes, ctx().stream));
+  return p;
+}
+
+void dev_free(void *p) { cudaFreeAsync(p, ctx().stream); }
+
 void Ctx::init() {
-  if (!stream) CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  if (!stream) {
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    CK(cudaDeviceGetDefaultMemPool(&pool, dev));
+    unsigned long long keep = ~0ull;  // keep freed blocks for reuse
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   memset(&stats, 0, sizeof(stats));
   kernel_launches = 0;
   const char *t = getenv("PARRSB_GPU_TIMING");
@@ -427,6 +443,12 @@ extern "C" void parrsb_gpu_finalize(void) {
     g_ws = nullptr;
   }
   if (g_ctx.stream) {
+    cudaStreamSynchronize(g_ctx.stream);
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+      cudaMemPoolTrimTo(pool, 0);
     cudaStreamDestroy(g_ctx.stream);
     g_ctx.stream = nullptr;
   }

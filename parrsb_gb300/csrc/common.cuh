@@ -46,6 +46,11 @@ struct ArgError {
 // Device buffer (RAII) and a per-thread context that owns the stream, event
 // pool and statistics of the current call.
 // --------------------------------------------------------------------------
+// Stream-ordered device allocation on the library stream (memory is kept in
+// the device's default pool between calls; see Ctx::init).
+void *dev_alloc(size_t bytes);
+void dev_free(void *p);
+
 template <typename T>
 struct DBuf {
   T *p = nullptr;
@@ -64,14 +69,14 @@ struct DBuf {
   void alloc(size_t count) {
     release();
     if (count == 0) count = 1;
-    CK(cudaMalloc((void **)&p, count * sizeof(T)));
+    p = (T *)dev_alloc(count * sizeof(T));
     n = count;
   }
   void ensure(size_t count) {
     if (count > n || p == nullptr) alloc(count);
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) dev_free(p);
     p = nullptr, n = 0;
   }
   ~DBuf() { release(); }

@@ -712,12 +712,12 @@ struct Lanczos {
     for (int it = 0; it < MI; it++) {
       tile<TM_P, GATE_RUN>(it);
       fin<FIN_PMEAN, GATE_RUN>(it);
-      if (!ev.empty()) CK(cudaEventRecord(ev[2 * it], st));
+      if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
       k_spmv<VT><<<T, LZ_THREADS, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p,
                                            lv.slice_off.p, lv.slice_w.p, p.p, w.p,
                                            part.p);
       CK_LAUNCH();
-      if (!ev.empty()) CK(cudaEventRecord(ev[2 * it + 1], st));
+      if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       fin<FIN_PAP, GATE_RUN>(it);
       tile<TM_R, GATE_RUN>(it);
