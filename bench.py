@@ -247,19 +247,14 @@ def main():
         assert rc == 0, rc
         return P.last_stats()
 
+    from parrsb_gb300 import replicas
+
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier(world)
         torch.cuda.synchronize()
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replicas.max_over_ranks(x, world)
 
     for _ in range(args.warmup):
         step_device()

@@ -98,6 +98,15 @@ PARRSB_API void fparrsb_conn_mesh(long long *vtx, double *coord, int *nel, int *
  * Extensions (no counterpart in the reference).
  * ---------------------------------------------------------------------- */
 
+/* parrsb_part_mesh that also returns seq[e], the position of element e
+ * inside part[e] in the final element order (the `seq` output documented in
+ * the reference's README.md:46-66).  For RCB / RIB this order is the one
+ * rcb_local / rib_local leave (src/rcb.c:39-72, src/rib.c:58-74); for RSB it
+ * is the order after the last bisection. */
+PARRSB_API int parrsb_part_mesh_seq(int *part, int *seq, const long long *vtx,
+                                    const double *xyz, const int *tag, int nel, int nv,
+                                    parrsb_options *options, int nparts);
+
 /* Same as parrsb_part_mesh / parrsb_conn_mesh with every array a DEVICE
  * pointer on the current device (inputs already resident in HBM). */
 PARRSB_API int parrsb_part_mesh_device(int *d_part, const long long *d_vtx,
@@ -141,6 +150,20 @@ enum {
 };
 
 PARRSB_API int parrsb_get_stats(parrsb_stats *out);
+
+/* Batched level solve: the Fiedler vector of every group of elements
+ * (group[e] in [0, ngroups); a group's elements in element order define its
+ * start vector, as the current order does inside RSB).  All groups run in
+ * the same kernel launches when batched != 0, one group at a time
+ * otherwise.  fiedler[e]: normalised Fiedler value of element e (0 for
+ * groups of one element); iters[g] / resid[g]: Lanczos steps and FP64
+ * eigen-residual ||L f - rho f|| / ||f|| of group g (may be NULL).  Uses
+ * rsb_max_iter, rsb_max_passes and rsb_tol of *options (environment
+ * overrides applied).  Host arrays. */
+PARRSB_API int parrsb_fiedler_groups(double *fiedler, long long *iters, double *resid,
+                                     const long long *vtx, const int *group, int nel,
+                                     int nv, int ngroups, parrsb_options *options,
+                                     int batched);
 
 /* Partition quality on the element dual graph (weight = shared vertices):
  * q[0] weighted edge cut, q[1] cut dual edges, q[2] cut face-sharing pairs,

@@ -28,7 +28,7 @@ LIB_PATH = os.path.join(HERE, "libparrsb_gb300.so")
 EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
            "fparrsb_conn_mesh", "parrsb_part_mesh_device",
            "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
-           "parrsb_gpu_finalize"]
+           "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq"]
 
 
 class ParrsbError(RuntimeError):
@@ -83,6 +83,9 @@ def library(build_if_missing=False):
     L.parrsb_part_mesh.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(ParrsbOptions), ctypes.c_int]
     L.parrsb_part_mesh.restype = ctypes.c_int
+    L.parrsb_part_mesh_seq.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ParrsbOptions), ctypes.c_int]
+    L.parrsb_part_mesh_seq.restype = ctypes.c_int
     L.parrsb_part_mesh_device.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int,
                                           ctypes.POINTER(ParrsbOptions),
                                           ctypes.c_int]
@@ -96,6 +99,9 @@ def library(build_if_missing=False):
     L.parrsb_get_stats.argtypes = [ctypes.POINTER(Stats)]
     L.parrsb_part_quality.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_int]
+    L.parrsb_fiedler_groups.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.POINTER(ParrsbOptions),
+                                        ctypes.c_int]
     L.parrsb_gpu_finalize.argtypes = []
     L.parrsb_gpu_finalize.restype = None
     _lib = L
@@ -135,6 +141,24 @@ def part_mesh(vtx, xyz, nparts, options=None, tag=None, **kw):
     return part
 
 
+def part_mesh_seq(vtx, xyz, nparts, **kw):
+    """parrsb_part_mesh_seq: (part, seq) where seq[e] is the position of
+    element e inside its part in the final order."""
+    kw.setdefault("verbose_level", 0)
+    options = ParrsbOptions.make(**kw)
+    nel = len(vtx) if vtx is not None else len(xyz)
+    nv = vtx.shape[1] if vtx is not None else xyz.shape[1]
+    vtx = None if vtx is None else np.ascontiguousarray(vtx, np.int64)
+    xyz = None if xyz is None else np.ascontiguousarray(xyz, np.float64)
+    part = np.full(nel, -1, np.int32)
+    seq = np.full(nel, -1, np.int32)
+    rc = library().parrsb_part_mesh_seq(_ptr(part), _ptr(seq), _ptr(vtx), _ptr(xyz), None,
+                                        nel, nv, ctypes.byref(options), nparts)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_part_mesh_seq")
+    return part, seq
+
+
 def conn_mesh(coord, ndim, tol=0.2, periodic=None):
     """Vertex ids from corner coordinates (parrsb_conn_mesh).  coord:
     (nel, nv, ndim) in Nek preprocessor corner order.  Returns (nel, nv)
@@ -166,6 +190,26 @@ def part_quality(part, vtx, nparts):
     return q
 
 
+def fiedler_groups(vtx, group, ngroups, batched=True, **kw):
+    """Batched level solve (parrsb_fiedler_groups): the Fiedler vector of
+    every group of elements.  Returns (fiedler[nel], iters[ngroups],
+    resid[ngroups])."""
+    kw.setdefault("verbose_level", 0)
+    options = ParrsbOptions.make(**kw)
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    group = np.ascontiguousarray(group, np.int32)
+    nel, nv = vtx.shape
+    f = np.zeros(nel, np.float64)
+    it = np.zeros(ngroups, np.int64)
+    rs = np.zeros(ngroups, np.float64)
+    rc = library().parrsb_fiedler_groups(_ptr(f), _ptr(it), _ptr(rs), _ptr(vtx),
+                                         _ptr(group), nel, nv, ngroups,
+                                         ctypes.byref(options), 1 if batched else 0)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_fiedler_groups")
+    return f, it, rs
+
+
 def last_stats():
     s = Stats()
     library().parrsb_get_stats(ctypes.byref(s))
@@ -177,7 +221,7 @@ def finalize():
         _lib.parrsb_gpu_finalize()
 
 
-__all__ = ["part_mesh", "conn_mesh", "part_quality", "last_stats",
+__all__ = ["part_mesh", "part_mesh_seq", "conn_mesh", "part_quality", "last_stats", "fiedler_groups",
            "default_options", "ParrsbOptions", "ParrsbError", "DEFAULTS",
            "library", "finalize", "OK", "ERR_ARGS", "ERR_CUDA", "ERR_CHECK",
            "ERR_UNSUPPORTED"]

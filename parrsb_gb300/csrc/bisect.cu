@@ -329,6 +329,279 @@ __global__ void k_part_from_segs(const int *__restrict__ perm,
   if (i < N) part[perm[i]] = r0[seg_of_pos[i]];
 }
 
+// ---------------------------------------------------------------------------
+// Whole-recursion RCB of one small segment per CTA (n <= SMALL_MAX).
+// Every recursion level of the segment runs inside the CTA: the sub-range of
+// position x at depth d follows from (n, p) alone (rank split at
+// lower_count(len, p) while p > 1, then, with LOCAL, halving at len / 2 as
+// rcb_local does), the bounding box of each sub-range comes from a warp-
+// segmented reduction (long sub-ranges, 64-bit atomics into a per-CTA
+// scratch) or a sequential loop (short ones), and the segmented stable sort
+// by (sub-range start, ordered key) is an LSD radix sort in shared memory
+// (warp w ranks items [512 w, 512 w + 512) in order with __match_any_sync).
+// Constant key bytes are skipped.  Gives exactly the order of the level-by-
+// level global path.
+// ---------------------------------------------------------------------------
+constexpr int SMALL_MAX = 8192;
+constexpr int SMALL_THREADS = 512;
+constexpr int SMALL_ITEMS = 16;  // SMALL_MAX / SMALL_THREADS
+
+struct SubR {
+  int st, len, p, rank;
+};
+
+template <bool LOCAL>
+__device__ __forceinline__ SubR descend(int x, int n, int p0, int d) {
+  SubR r{0, n, p0, 0};
+  for (int k = 0; k < d; k++) {
+    int L, h;
+    if (r.p > 1) {
+      L = (int)lower_count(r.len, r.p);
+      h = (r.p + 1) / 2;
+    } else if (LOCAL && r.len >= 2) {
+      L = r.len / 2;
+      h = 0;
+    } else {
+      continue;  // finished sub-range keeps its place
+    }
+    if (x < r.st + L) {
+      r.len = L;
+      r.p = r.p > 1 ? h : r.p;
+    } else {
+      r.st += L;
+      r.len -= L;
+      r.rank += h;
+      r.p = r.p > 1 ? r.p - h : r.p;
+    }
+  }
+  return r;
+}
+
+template <bool LOCAL>
+__device__ __forceinline__ bool sub_active(const SubR &r) {
+  return r.p > 1 || (LOCAL && r.len >= 2);
+}
+
+__device__ __forceinline__ double key_to_double(unsigned long long k) {
+  unsigned long long b = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+
+template <bool LOCAL>
+__global__ void __launch_bounds__(SMALL_THREADS)
+k_rcb_small(int *__restrict__ perm, const double *__restrict__ cent, ll N, int ndim,
+            const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
+            const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
+            unsigned long long *__restrict__ scratch, int *__restrict__ part) {
+  extern __shared__ unsigned long long smem_u64[];
+  u64 *key = smem_u64;                                   // SMALL_MAX
+  u64 *key2 = key + SMALL_MAX;                            // SMALL_MAX
+  unsigned *item = (unsigned *)(key2 + SMALL_MAX);        // (st << 16) | ord
+  unsigned *item2 = item + SMALL_MAX;
+  unsigned short *wcnt = (unsigned short *)(item2 + SMALL_MAX);  // [16][256]
+  __shared__ unsigned dbase[256];
+  __shared__ unsigned long long s_and, s_or;
+  __shared__ unsigned s_stand, s_stor;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ll sg = blockIdx.x;
+  const ll start = seg_start[sg];
+  const int n = (int)seg_n[sg], p0 = seg_p[sg], r0 = seg_r0[sg];
+  bool seg_act = p0 > 1 || (LOCAL && p0 == 1 && n >= 2);
+  if (n <= 0 || p0 <= 0) return;
+  if (!seg_act || n > SMALL_MAX) {
+    if (part && n <= SMALL_MAX && p0 == 1)
+      for (int x = threadIdx.x; x < n; x += blockDim.x) part[perm[start + x]] = r0;
+    return;
+  }
+  unsigned long long *sc = scratch + start * 6;  // slot = global position of the sub-range start
+  for (int x = threadIdx.x; x < n; x += blockDim.x) item[x] = (unsigned)x;
+  __syncthreads();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (int d = 0; d < 64; d++) {
+    // ---- sub-range of each position at depth d
+    bool any = false;
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      int x = warp * 512 + r * 32 + lane;
+      if (x < n) any |= sub_active<LOCAL>(descend<LOCAL>(x, n, p0, d));
+    }
+    if (!__syncthreads_or(any)) break;
+    // ---- clear bbox slots of active sub-ranges (slot = sub-range start)
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      int x = warp * 512 + r * 32 + lane;
+      if (x < n) {
+        SubR sr = descend<LOCAL>(x, n, p0, d);
+        if (sr.st == x && sub_active<LOCAL>(sr) && sr.len > 32) {
+          for (int q = 0; q < 3; q++) sc[6 * x + q] = ~0ull, sc[6 * x + 3 + q] = 0ull;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- bounding boxes
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      int x = warp * 512 + r * 32 + lane;
+      bool valid = x < n;
+      SubR sr = valid ? descend<LOCAL>(x, n, p0, d) : SubR{-1, 0, 0, 0};
+      bool act = valid && sub_active<LOCAL>(sr);
+      if (act && sr.len <= 32) {
+        if (sr.st == x) {  // sequential box of a short sub-range
+          u64 mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
+          for (int y = x; y < x + sr.len; y++) {
+            int e = perm[start + (item[y] & 0xFFFF)];
+            for (int q = 0; q < 3; q++) {
+              u64 k = ordered_key(cent[(ll)q * N + e]);
+              mn[q] = k < mn[q] ? k : mn[q];
+              mx[q] = k > mx[q] ? k : mx[q];
+            }
+          }
+          for (int q = 0; q < 3; q++) sc[6 * x + q] = mn[q], sc[6 * x + 3 + q] = mx[q];
+        }
+      }
+      // warp-segmented reduction for long sub-ranges
+      bool lng = act && sr.len > 32;
+      int segkey = lng ? sr.st : -1 - lane;  // unique key for lanes not taking part
+      u64 mn[3], mx[3];
+      int e = lng ? perm[start + (item[x] & 0xFFFF)] : 0;
+      for (int q = 0; q < 3; q++) {
+        u64 k = lng ? ordered_key(cent[(ll)q * N + e]) : 0ull;
+        mn[q] = lng ? k : ~0ull;
+        mx[q] = k;
+      }
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        int ok = __shfl_down_sync(0xffffffffu, segkey, off);
+        bool same = (lane + off < 32) && ok == segkey;
+        for (int q = 0; q < 3; q++) {
+          u64 a = __shfl_down_sync(0xffffffffu, mn[q], off);
+          u64 b = __shfl_down_sync(0xffffffffu, mx[q], off);
+          if (same) {
+            mn[q] = a < mn[q] ? a : mn[q];
+            mx[q] = b > mx[q] ? b : mx[q];
+          }
+        }
+      }
+      // after the down-sweep the first lane of each run holds the run's box
+      int prevkey = __shfl_up_sync(0xffffffffu, segkey, 1);
+      bool head = lane == 0 || prevkey != segkey;
+      if (lng && head) {
+        for (int q = 0; q < 3; q++) {
+          atomicMin(&sc[6 * sr.st + q], mn[q]);
+          atomicMax(&sc[6 * sr.st + 3 + q], mx[q]);
+        }
+      }
+    }
+    __syncthreads();
+    // ---- keys along each sub-range's longest axis
+    if (threadIdx.x == 0) s_and = ~0ull, s_or = 0ull, s_stand = ~0u, s_stor = 0u;
+    __syncthreads();
+    u64 kand = ~0ull, kor = 0ull;
+    unsigned stand = ~0u, stor = 0u;
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      int x = warp * 512 + r * 32 + lane;
+      if (x >= n) continue;
+      SubR sr = descend<LOCAL>(x, n, p0, d);
+      u64 k = 0ull;
+      if (sub_active<LOCAL>(sr)) {
+        double len[3];
+        for (int q = 0; q < ndim; q++)
+          len[q] = __dsub_rn(key_to_double(sc[6 * sr.st + 3 + q]), key_to_double(sc[6 * sr.st + q]));
+        int ax = 0;
+        for (int q = 1; q < ndim; q++)
+          if (len[q] > len[ax]) ax = q;
+        int e = perm[start + (item[x] & 0xFFFF)];
+        k = ordered_key(cent[(ll)ax * N + e]);
+      }
+      key[x] = k;
+      item[x] = ((unsigned)sr.st << 16) | (item[x] & 0xFFFF);
+      kand &= k, kor |= k;
+      stand &= (unsigned)sr.st, stor |= (unsigned)sr.st;
+    }
+    atomicAnd(&s_and, kand);
+    atomicOr(&s_or, kor);
+    atomicAnd(&s_stand, stand);
+    atomicOr(&s_stor, stor);
+    __syncthreads();
+    u64 kdiff = s_and ^ s_or;
+    unsigned sdiff = s_stand ^ s_stor;
+    // ---- stable LSD passes: key bytes, then sub-range start bytes
+    for (int b = 0; b < 10; b++) {
+      bool is_st = b >= 8;
+      int shift = is_st ? 8 * (b - 8) : 8 * b;
+      if (is_st ? ((sdiff >> shift) & 255u) == 0 : ((kdiff >> shift) & 255ull) == 0) continue;
+      for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) wcnt[i] = 0;
+      __syncthreads();
+      unsigned rk[SMALL_ITEMS], dg[SMALL_ITEMS];
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        int x = warp * 512 + r * 32 + lane;
+        unsigned dgt = 256;
+        if (x < n)
+          dgt = is_st ? ((item[x] >> 16) >> shift) & 255u : (unsigned)(key[x] >> shift) & 255u;
+        unsigned peers = __match_any_sync(0xffffffffu, dgt);
+        unsigned before = 0;
+        if (dgt < 256) before = wcnt[warp * 256 + dgt];
+        __syncwarp();
+        if (dgt < 256) {
+          rk[r] = before + __popc(peers & lt_mask);
+          if (lane == __ffs(peers) - 1) wcnt[warp * 256 + dgt] = (unsigned short)(before + __popc(peers));
+        }
+        dg[r] = dgt;
+        __syncwarp();
+      }
+      __syncthreads();
+      if (threadIdx.x < 256) {
+        unsigned run = 0;
+        for (int w = 0; w < 16; w++) {
+          unsigned t = wcnt[w * 256 + threadIdx.x];
+          wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
+          run += t;
+        }
+        dbase[threadIdx.x] = run;  // total of this digit (scanned below)
+      }
+      __syncthreads();
+      if (threadIdx.x < 32) {  // exclusive scan of the 256 digit totals
+        unsigned v[8], s2 = 0;
+        for (int j = 0; j < 8; j++) v[j] = dbase[threadIdx.x * 8 + j], s2 += v[j];
+        unsigned incl = s2;
+        for (int o = 1; o < 32; o <<= 1) {
+          unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (threadIdx.x >= o) incl += y;
+        }
+        unsigned run = incl - s2;
+        for (int j = 0; j < 8; j++) dbase[threadIdx.x * 8 + j] = run, run += v[j];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        int x = warp * 512 + r * 32 + lane;
+        if (x < n) {
+          unsigned pos = dbase[dg[r]] + wcnt[warp * 256 + dg[r]] + rk[r];
+          key2[pos] = key[x];
+          item2[pos] = item[x];
+        }
+      }
+      __syncthreads();
+      for (int x = threadIdx.x; x < n; x += blockDim.x) key[x] = key2[x], item[x] = item2[x];
+      __syncthreads();
+    }
+    for (int x = threadIdx.x; x < n; x += blockDim.x) item[x] &= 0xFFFF;
+    __syncthreads();
+  }
+  // ---- write the order (and ranks) back
+  int *tmp = (int *)key2;
+  for (int x = threadIdx.x; x < n; x += blockDim.x) tmp[x] = perm[start + (item[x] & 0xFFFF)];
+  __syncthreads();
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    perm[start + x] = tmp[x];
+    if (part) part[tmp[x]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+  }
+}
+
+__global__ void k_max_active_n(const int *__restrict__ p, const ll *__restrict__ n, ll nseg,
+                               int do_local, unsigned long long *__restrict__ mx) {
+  ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < nseg && seg_active(p[s], n[s], do_local)) atomicMax(mx, (unsigned long long)n[s]);
+}
+
 // Run the tile tree over every segment of `t` until one value per segment
 // is left; result in out_final (nseg * V values).
 template <int V, int GEN0, bool BBOX>
@@ -391,17 +664,41 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
   ws.keys.ensure((size_t)N);
   ws.vals.ensure((size_t)N);
   DBuf<int> nact_d(1);
+  DBuf<unsigned long long> maxn_d(1);
+  const size_t small_smem = (size_t)SMALL_MAX * (8 + 8 + 4 + 4) + 16 * 256 * 2;
   for (int level = 0; level < 200; level++) {
     ll nseg = t.count;
-    // active segments and children counts
+    // active segments, their largest size, and children counts
     ws.child_cnt.ensure((size_t)nseg);
     CK(cudaMemsetAsync(nact_d.p, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(maxn_d.p, 0, sizeof(unsigned long long), st));
     k_child_counts<<<grid_for(nseg, 256), 256, 0, st>>>(t.p.p, t.n.p, nseg, do_local,
                                                         ws.child_cnt.p, nact_d.p);
     CK_LAUNCH();
+    k_max_active_n<<<grid_for(nseg, 256), 256, 0, st>>>(t.p.p, t.n.p, nseg, do_local, maxn_d.p);
+    CK_LAUNCH();
     int nact = 0;
+    unsigned long long maxn = 0;
     d2h(&nact, nact_d.p, 1);
+    d2h(&maxn, maxn_d.p, 1);
     sync();
+    if (kind == BISECT_RCB && nact > 0 && maxn <= (unsigned long long)SMALL_MAX) {
+      // every remaining level of every segment in one launch
+      DBuf<unsigned long long> scratch((size_t)N * 6);
+      if (do_local) {
+        CK(cudaFuncSetAttribute(k_rcb_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)small_smem));
+        k_rcb_small<true><<<(unsigned)nseg, SMALL_THREADS, small_smem, st>>>(
+            perm.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p, scratch.p, part_of_elem);
+      } else {
+        CK(cudaFuncSetAttribute(k_rcb_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)small_smem));
+        k_rcb_small<false><<<(unsigned)nseg, SMALL_THREADS, small_smem, st>>>(
+            perm.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p, scratch.p, part_of_elem);
+      }
+      CK_LAUNCH();
+      return;
+    }
     fill_seg_of_pos(t, ws.seg_of_pos.p, N);
     if (nact == 0) break;
     ws.axis.ensure((size_t)nseg);

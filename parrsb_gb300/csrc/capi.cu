@@ -175,8 +175,26 @@ __global__ void k_block_part(int *part, ll nel, int nparts) {
 }
 
 // Device-resident partitioning: inputs and output already in HBM.
+__global__ void k_seq_from_order(const int *__restrict__ perm, const int *__restrict__ part,
+                                 ll N, int *__restrict__ first, int *__restrict__ seq) {
+  // parts are contiguous and in rank order in the final element order
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int e = perm[i];
+  int r = part[e];
+  if (i == 0 || part[perm[i - 1]] != r) first[r] = (int)i;
+}
+
+__global__ void k_seq_write(const int *__restrict__ perm, const int *__restrict__ part, ll N,
+                            const int *__restrict__ first, int *__restrict__ seq) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int e = perm[i];
+  seq[e] = (int)(i - first[part[e]]);
+}
+
 void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int nel, int nv,
-                   const parrsb_options *o, int nparts) {
+                   const parrsb_options *o, int nparts, int *d_seq = nullptr) {
   cudaStream_t st = ctx().stream;
   if (nel == 0) return;
   int ndim = (nv == 8) ? 3 : 2;
@@ -205,7 +223,14 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     h2d(t.r0.p, &r00, 1);
     t.count = 1;
     bisect_segments(o->partitioner == 1 ? BISECT_RCB : BISECT_RIB, perm, t, W.cent.p, N, ndim,
-                    false, d_part, bws);
+                    d_seq != nullptr, d_part, bws);
+    if (d_seq) {
+      DBuf<int> first((size_t)P);
+      k_seq_from_order<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
+      CK_LAUNCH();
+      k_seq_write<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
+      CK_LAUNCH();
+    }
     sync();
   } else if (o->partitioner == 0) {
     RsbOpts ro;
@@ -218,11 +243,21 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.fp32 = env_int("PARRSB_GPU_FP32", 0);
     ro.check_resid = env_int("PARRSB_GPU_CHECK_RESID", 1);
     ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
-    rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part);
+    rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq);
     sync();
   } else {
     k_block_part<<<grid_for(N, 256), 256, 0, st>>>(d_part, N, nparts);
     CK_LAUNCH();
+    if (d_seq) {  // elements stay in input order inside their block
+      DBuf<int> perm((size_t)N), first((size_t)nparts);
+      std::vector<int> h(N);
+      for (ll i = 0; i < N; i++) h[i] = (int)i;
+      h2d(perm.p, h.data(), N);
+      k_seq_from_order<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
+      CK_LAUNCH();
+      k_seq_write<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
+      CK_LAUNCH();
+    }
     sync();
   }
 }
@@ -271,9 +306,26 @@ void maybe_fault(const char *stage) {
 
 using namespace prsb;
 
+static int part_mesh_host(int *part, int *seq, const long long *vtx, const double *xyz,
+                          const int *tag, int nel, int nv, parrsb_options *options,
+                          int nparts);
+
 extern "C" int parrsb_part_mesh(int *part, const long long *vtx, const double *xyz,
                                 const int *tag, int nel, int nv, parrsb_options *options,
                                 int nparts) {
+  return part_mesh_host(part, nullptr, vtx, xyz, tag, nel, nv, options, nparts);
+}
+
+extern "C" int parrsb_part_mesh_seq(int *part, int *seq, const long long *vtx,
+                                    const double *xyz, const int *tag, int nel, int nv,
+                                    parrsb_options *options, int nparts) {
+  if (nel > 0 && !seq) return PARRSB_ERR_ARGS;
+  return part_mesh_host(part, seq, vtx, xyz, tag, nel, nv, options, nparts);
+}
+
+static int part_mesh_host(int *part, int *seq, const long long *vtx, const double *xyz,
+                          const int *tag, int nel, int nv, parrsb_options *options,
+                          int nparts) {
   auto t0 = std::chrono::steady_clock::now();
   int rc = prepare_options(vtx, xyz, nel, nv, options, nparts, tag, true);
   if (rc != PARRSB_OK) return rc;
@@ -297,12 +349,15 @@ extern "C" int parrsb_part_mesh(int *part, const long long *vtx, const double *x
       W.part.ensure((size_t)N);
     }
     maybe_fault("upload");
+    DBuf<int> dseq;
+    if (seq) dseq.alloc((size_t)N);
     part_mesh_dev(W.part.p, vtx ? W.vtx.p : nullptr, xyz ? W.xyz.p : nullptr, nel, nv, options,
-                  nparts);
+                  nparts, seq ? dseq.p : nullptr);
     maybe_fault("partition");
     {
       StageTimer tm(PARRSB_STAGE_DOWNLOAD);
       d2h(part, W.part.p, (size_t)N);
+      if (seq) d2h(seq, dseq.p, (size_t)N);
     }
     sync();
     return PARRSB_OK;
@@ -413,6 +468,45 @@ extern "C" int parrsb_get_stats(parrsb_stats *out) {
   if (!out) return PARRSB_ERR_ARGS;
   *out = ctx().stats;
   return PARRSB_OK;
+}
+
+extern "C" int parrsb_fiedler_groups(double *fiedler, long long *iters, double *resid,
+                                     const long long *vtx, const int *group, int nel, int nv,
+                                     int ngroups, parrsb_options *options, int batched) {
+  if (!options || nel < 0 || nv < 1 || nv > 8 || ngroups < 1) return PARRSB_ERR_ARGS;
+  if (nel > 0 && (!fiedler || !vtx || !group)) return PARRSB_ERR_ARGS;
+  update_options(options);
+  for (int e = 0; e < nel; e++)
+    if (group[e] < 0 || group[e] >= ngroups) return PARRSB_ERR_ARGS;
+  return guarded([&]() -> int {
+    ctx().init();
+    ll N = nel;
+    std::vector<long long> it(ngroups, 0);
+    std::vector<double> rs(ngroups, 0.0);
+    if (N > 0) {
+      DBuf<long long> dv((size_t)N * nv);
+      DBuf<int> dg((size_t)N);
+      DBuf<double> df((size_t)N);
+      h2d(dv.p, vtx, (size_t)N * nv);
+      h2d(dg.p, group, (size_t)N);
+      RsbOpts ro;
+      ro.miter = options->rsb_max_iter;
+      ro.mpass = options->rsb_max_passes;
+      ro.tol = options->rsb_tol;
+      ro.fp32 = env_int("PARRSB_GPU_FP32", 0);
+      ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
+      ro.batched = batched ? 1 : 0;
+      fiedler_groups_device(dv.p, N, nv, dg.p, ngroups, ro, df.p, it.data(), rs.data());
+      d2h(fiedler, df.p, (size_t)N);
+      sync();
+    }
+    if (iters)
+      for (int g = 0; g < ngroups; g++) iters[g] = it[g];
+    if (resid)
+      for (int g = 0; g < ngroups; g++) resid[g] = rs[g];
+    ctx().stats.kernel_launches = ctx().kernel_launches;
+    return PARRSB_OK;
+  });
 }
 
 extern "C" int parrsb_part_quality(double *q, const int *part, const long long *vtx, int nel,

@@ -224,6 +224,48 @@ __device__ __forceinline__ double initv_formula(ll li, ll n) {
   return v;
 }
 
+
+// Per-thread accumulators for the tile dot products.  FP64 vectors use a
+// plain FMA chain.  FP32 vectors keep a compensated (TwoSum / TwoProduct)
+// FP32 pair, so the partial sums carry ~48 significant bits without using
+// GB300's low-throughput FP64 pipe per row; partials are combined in FP64.
+template <typename VT>
+struct Acc;
+
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ void add_prod(double a, double b) { s = fma(a, b, s); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+template <>
+struct Acc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void two_sum(float x) {
+    float t = s + x;
+    float bp = t - s;
+    float e = (s - (t - bp)) + (x - bp);
+    s = t;
+    c += e;
+  }
+  __device__ __forceinline__ void add(float x) { two_sum(x); }
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    two_sum(p);
+    c += e;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// Small non-negative integer (< 2^23) to float without a conversion
+// instruction: 2^23 + w has w in the low mantissa bits.
+__device__ __forceinline__ float small_u2f(unsigned w) {
+  return __int_as_float(0x4B000000 | w) - 8388608.0f;
+}
+
 // Generic per-tile pass.  MODE selects the element-wise work.
 enum TileMode {
   TM_IV_SUM = 0,     // sum of initv formula
@@ -236,7 +278,7 @@ enum TileMode {
   TM_SUB_C = 7,      // f -= c
   TM_SQ_F = 8,       // sum f^2
   TM_SCALE_F = 9,    // f *= c
-  TM_RESID1 = 10,    // y = L f in FP64 -> w64; sums f.y, f.f
+  TM_RESID1 = 10,    // y = L f in FP64 -> y64; sums f.y, f.f
   TM_RESID2 = 11,    // sum (y - rho f)^2
   TM_SUM_F_WARM = 12 // same as TM_SUM_F but for a warm start vector
 };
@@ -254,42 +296,41 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   int g = tgrp[t];
   const GState &s = gs[g];
   if (!gate_ok(s, GATE)) return;
-  double acc = 0.0, acc2 = 0.0;
+  Acc<VT> acc;
+  double dacc = 0.0, dacc2 = 0.0;  // FP64 accumulators of the setup passes
+  const VT c = (VT)s.c, beta = (VT)s.beta, alpha = (VT)s.alpha;
   ll b = tbeg[t], e = tend[t];
   for (ll i = b + threadIdx.x; i < e; i += blockDim.x) {
     if (MODE == TM_IV_SUM) {
-      acc = __dadd_rn(acc, initv_formula(i - s.start, s.n));
+      dacc = __dadd_rn(dacc, initv_formula(i - s.start, s.n));
     } else if (MODE == TM_IV_SQ) {
       double v = __dsub_rn(initv_formula(i - s.start, s.n), s.c);
-      acc = __dadd_rn(acc, __dmul_rn(v, v));
+      dacc = __dadd_rn(dacc, __dmul_rn(v, v));
     } else if (MODE == TM_IV_WRITE) {
       double v = __dsub_rn(initv_formula(i - s.start, s.n), s.c);
       f[i] = (VT)__dmul_rn(v, s.alpha);
     } else if (MODE == TM_SUM_F || MODE == TM_SUM_F_WARM) {
-      acc = __dadd_rn(acc, (double)f[i]);
+      acc.add(f[i]);
     } else if (MODE == TM_INIT_R) {
-      VT q = (VT)__dsub_rn((double)f[i], s.c);
+      VT q = f[i] - c;
       r[i] = q;
       V[i] = q;
-      acc = __dadd_rn(acc, __dmul_rn((double)q, (double)q));
+      acc.add_prod(q, q);
     } else if (MODE == TM_P) {
-      double pv = it == 0 ? (double)r[i]
-                          : __dadd_rn(__dmul_rn(s.beta, __dsub_rn((double)p[i], s.c)),
-                                      (double)r[i]);
-      VT q = (VT)pv;
+      VT q = it == 0 ? r[i] : (VT)fma(beta, p[i] - c, r[i]);
       p[i] = q;
-      acc = __dadd_rn(acc, (double)q);
+      acc.add(q);
     } else if (MODE == TM_R) {
-      VT q = (VT)__dsub_rn((double)r[i], __dmul_rn(s.alpha, (double)w[i]));
+      VT q = (VT)fma(-alpha, w[i], r[i]);
       r[i] = q;
       V[(ll)(it + 1) * N + i] = q;
-      acc = __dadd_rn(acc, __dmul_rn((double)q, (double)q));
+      acc.add_prod(q, q);
     } else if (MODE == TM_SUB_C) {
-      f[i] = (VT)__dsub_rn((double)f[i], s.c);
+      f[i] = f[i] - c;
     } else if (MODE == TM_SQ_F) {
-      acc = __dadd_rn(acc, __dmul_rn((double)f[i], (double)f[i]));
+      acc.add_prod(f[i], f[i]);
     } else if (MODE == TM_SCALE_F) {
-      f[i] = (VT)__dmul_rn((double)f[i], s.c);
+      f[i] = (VT)((double)f[i] * s.c);
     } else if (MODE == TM_RESID1) {
       double fi = (double)f[i];
       ll sl = i >> 5;
@@ -301,26 +342,31 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         yv = __dadd_rn(yv, __dmul_rn((double)(x >> 28), __dsub_rn(fi, (double)f[x & 0x0FFFFFFFu])));
       }
       y64[i] = yv;
-      acc = __dadd_rn(acc, __dmul_rn(fi, yv));
-      acc2 = __dadd_rn(acc2, __dmul_rn(fi, fi));
+      dacc = __dadd_rn(dacc, __dmul_rn(fi, yv));
+      dacc2 = __dadd_rn(dacc2, __dmul_rn(fi, fi));
     } else if (MODE == TM_RESID2) {
       double v = __dsub_rn(y64[i], __dmul_rn(s.c, (double)f[i]));
-      acc = __dadd_rn(acc, __dmul_rn(v, v));
+      dacc = __dadd_rn(dacc, __dmul_rn(v, v));
     }
   }
   constexpr bool has_sum = !(MODE == TM_IV_WRITE || MODE == TM_SUB_C || MODE == TM_SCALE_F);
+  constexpr bool fp64_setup = (MODE == TM_IV_SUM || MODE == TM_IV_SQ || MODE == TM_RESID1 ||
+                               MODE == TM_RESID2);
   if (has_sum) {
-    double tot = block_sum(acc, sh);
+    double tot = block_sum(fp64_setup ? dacc : acc.value(), sh);
     if (MODE == TM_RESID1) {
       __syncthreads();
-      double tot2 = block_sum(acc2, sh);
+      double tot2 = block_sum(dacc2, sh);
       if (threadIdx.x == 0) part[2 * t + 1] = tot2;
     }
     if (threadIdx.x == 0) part[(MODE == TM_RESID1 ? 2 : 1) * t] = tot;
   }
 }
 
-// w = L p in difference form, sum w_i (p_i - c) per tile.
+// w = L p and sum w_i (p_i - c) per tile.  FP32: difference form
+// w_i = sum_j w_ij (p_i - p_j) with FFMA.  FP64: w_i = d_i p_i - sum_j w_ij p_j
+// (the gather-scatter form of the reference, src/laplacian.c:188-205) with
+// one DFMA per nonzero and the weights taken from a shared-memory table.
 template <typename VT>
 __global__ void __launch_bounds__(LZ_THREADS)
 k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
@@ -329,37 +375,69 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        const int *__restrict__ slice_w, const VT *__restrict__ p, VT *__restrict__ w,
        double *__restrict__ part) {
   __shared__ double sh[32];
+  __shared__ double wlut[16];
+  if (threadIdx.x < 16) wlut[threadIdx.x] = (double)threadIdx.x;
+  __syncthreads();
   int t = blockIdx.x;
   int g = tgrp[t];
   if (!gs[g].run) return;
-  double c = gs[g].c;
-  double acc = 0.0;
+  const VT c = (VT)gs[g].c;
+  Acc<VT> acc;
   ll b = tbeg[t], e = tend[t];
   for (ll i = b + threadIdx.x; i < e; i += blockDim.x) {
     VT pi = p[i];
     ll sl = i >> 5;
     const unsigned *ep = ell + slice_off[sl] + (i & 31);
     int wd = slice_w[sl];
-    VT sum = (VT)0;
-    int k = 0;
-    for (; k + 4 <= wd; k += 4) {
-      unsigned x0 = __ldg(ep + (ll)(k + 0) * 32), x1 = __ldg(ep + (ll)(k + 1) * 32);
-      unsigned x2 = __ldg(ep + (ll)(k + 2) * 32), x3 = __ldg(ep + (ll)(k + 3) * 32);
-      VT p0 = p[x0 & 0x0FFFFFFFu], p1 = p[x1 & 0x0FFFFFFFu];
-      VT p2 = p[x2 & 0x0FFFFFFFu], p3 = p[x3 & 0x0FFFFFFFu];
-      sum += (VT)(x0 >> 28) * (pi - p0);
-      sum += (VT)(x1 >> 28) * (pi - p1);
-      sum += (VT)(x2 >> 28) * (pi - p2);
-      sum += (VT)(x3 >> 28) * (pi - p3);
+    VT y;
+    if (sizeof(VT) == 4) {
+      float sum = 0.f;
+      int k = 0;
+#pragma unroll 1
+      for (; k + 8 <= wd; k += 8) {
+        unsigned x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = __ldg(ep + (ll)(k + u) * 32);
+        float pj[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) pj[u] = (float)p[x[u] & 0x0FFFFFFFu];
+#pragma unroll
+        for (int u = 0; u < 8; u++) sum = fmaf(small_u2f(x[u] >> 28), (float)pi - pj[u], sum);
+      }
+      for (; k < wd; k++) {
+        unsigned x = __ldg(ep + (ll)k * 32);
+        sum = fmaf(small_u2f(x >> 28), (float)pi - (float)p[x & 0x0FFFFFFFu], sum);
+      }
+      y = (VT)sum;
+    } else {
+      double sum = 0.0;
+      unsigned dsum = 0;
+      int k = 0;
+#pragma unroll 1
+      for (; k + 8 <= wd; k += 8) {
+        unsigned x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = __ldg(ep + (ll)(k + u) * 32);
+        double pj[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) pj[u] = (double)p[x[u] & 0x0FFFFFFFu];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          sum = fma(wlut[x[u] >> 28], pj[u], sum);
+          dsum += x[u] >> 28;
+        }
+      }
+      for (; k < wd; k++) {
+        unsigned x = __ldg(ep + (ll)k * 32);
+        sum = fma(wlut[x >> 28], (double)p[x & 0x0FFFFFFFu], sum);
+        dsum += x >> 28;
+      }
+      y = (VT)fma((double)dsum, (double)pi, -sum);
     }
-    for (; k < wd; k++) {
-      unsigned x = __ldg(ep + (ll)k * 32);
-      sum += (VT)(x >> 28) * (pi - p[x & 0x0FFFFFFFu]);
-    }
-    w[i] = sum;
-    acc = __dadd_rn(acc, __dmul_rn((double)sum, __dsub_rn((double)pi, c)));
+    w[i] = y;
+    acc.add_prod(y, pi - c);
   }
-  double tot = block_sum(acc, sh);
+  double tot = block_sum(acc.value(), sh);
   if (threadIdx.x == 0) part[t] = tot;
 }
 
@@ -983,6 +1061,12 @@ __global__ void k_part_scatter(const int *__restrict__ perm, const int *__restri
   if (i < N) part[perm[i]] = grp[i];
 }
 
+__global__ void k_seq_rel(const int *__restrict__ perm, const int *__restrict__ gstart, ll N,
+                          int *__restrict__ seq) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) seq[perm[i]] = (int)(i - gstart[i]);
+}
+
 __global__ void k_fill_grp(const ll *__restrict__ gstart, const ll *__restrict__ gn,
                            const int *__restrict__ gid, int ng, int *__restrict__ grp) {
   // one block per group, loop over its range
@@ -1112,7 +1196,7 @@ void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g, SortWs &
 
 template <typename VT>
 static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, int P,
-                     const RsbOpts &o, int *d_part) {
+                     const RsbOpts &o, int *d_part, int *d_seq) {
   cudaStream_t st = ctx().stream;
   int ndim = (nv == 8) ? 3 : 2;
   parrsb_stats &S = ctx().stats;
@@ -1403,16 +1487,136 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
   fill_groups(st_, n_, r_, grp.p, N);
   k_part_scatter<<<grid_for(N, 256), 256, 0, st>>>(perm.p, grp.p, N, d_part);
   CK_LAUNCH();
+  if (d_seq) {
+    std::vector<int> pos_;
+    for (auto &g : groups) pos_.push_back((int)g.start);
+    fill_groups(st_, n_, pos_, segpos.p, N);
+    k_seq_rel<<<grid_for(N, 256), 256, 0, st>>>(perm.p, segpos.p, N, d_seq);
+    CK_LAUNCH();
+  }
 }
 
-void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv, int P,
-                const RsbOpts &o, int *d_part) {
+__global__ void k_group_keys(const int *__restrict__ group_of, ll N, u64 *__restrict__ keys,
+                             int *__restrict__ vals, int *__restrict__ cnt) {
+  ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= N) return;
+  int g = group_of[e];
+  keys[e] = (u64)(unsigned)g;
+  vals[e] = (int)e;
+  atomicAdd(&cnt[g], 1);
+}
+
+__global__ void k_scatter_f(const int *__restrict__ perm, const double *__restrict__ f_pos,
+                            ll N, double *__restrict__ f) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) f[perm[i]] = f_pos[i];
+}
+
+template <typename VT>
+static void fiedler_groups_impl(const long long *d_vtx, ll N, int nv, const int *d_group_of,
+                                int ngroups, const RsbOpts &o, double *d_f, long long *iters,
+                                double *resid) {
+  cudaStream_t st = ctx().stream;
+  SortWs sws;
+  Graph G;
+  {
+    StageTimer tm(PARRSB_STAGE_SETUP);
+    build_dual_graph(d_vtx, N, nv, G, sws);
+  }
+  if (G.max_w >= 16 || N >= (1ll << 28))
+    throw ArgError{PARRSB_ERR_UNSUPPORTED, "dual-graph weight >= 16 or more than 2^28 elements"};
+  // order elements by group (stable: element order inside a group)
+  DBuf<u64> keys((size_t)N);
+  DBuf<int> perm((size_t)N), cnt((size_t)ngroups), inv((size_t)N), grp((size_t)N);
+  CK(cudaMemsetAsync(cnt.p, 0, (size_t)ngroups * sizeof(int), st));
+  k_group_keys<<<grid_for(N, 256), 256, 0, st>>>(d_group_of, N, keys.p, perm.p, cnt.p);
+  CK_LAUNCH();
+  seg_sort_pairs(keys, perm, N, nullptr, 1, sws);
+  std::vector<int> hc(ngroups);
+  d2h(hc.data(), cnt.p, ngroups);
+  sync();
+  std::vector<ll> ast, an, all_st, all_n;
+  std::vector<int> act_id, gidx;
+  ll pos = 0;
+  for (int g = 0; g < ngroups; g++) {
+    all_st.push_back(pos), all_n.push_back(hc[g]);
+    if (hc[g] >= 2) {
+      act_id.push_back((int)ast.size());
+      gidx.push_back(g);
+      ast.push_back(pos), an.push_back(hc[g]);
+    } else {
+      act_id.push_back(-1);
+    }
+    pos += hc[g];
+  }
+  fill_groups(all_st, all_n, act_id, grp.p, N);
+  k_inv_perm<<<grid_for(N, 256), 256, 0, st>>>(perm.p, N, inv.p);
+  CK_LAUNCH();
+  Level lv;
+  {
+    StageTimer tm(PARRSB_STAGE_RESTRICT);
+    build_level(G, perm.p, inv.p, grp.p, N, lv);
+  }
+  DBuf<double> f_pos((size_t)N);
+  CK(cudaMemsetAsync(f_pos.p, 0, (size_t)N * sizeof(double), st));
+  for (int g = 0; g < ngroups; g++) iters[g] = 0, resid[g] = 0.0;
+  Lanczos<VT> lz;
+  auto collect = [&](const std::vector<GState> &res, const std::vector<int> &which) {
+    for (size_t q = 0; q < res.size(); q++) {
+      int g = gidx[which[q]];
+      iters[g] = res[q].total_iters;
+      resid[g] = res[q].resid;
+      ctx().stats.lanczos_iters += res[q].total_iters;
+      ctx().stats.lanczos_row_iters += res[q].total_iters * res[q].n;
+      if (res[q].resid > ctx().stats.max_fiedler_resid)
+        ctx().stats.max_fiedler_resid = res[q].resid;
+    }
+  };
+  if (ast.empty()) {
+  } else if (o.batched) {
+    std::vector<GState> res;
+    run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res);
+    std::vector<int> which(ast.size());
+    for (size_t q = 0; q < which.size(); q++) which[q] = (int)q;
+    collect(res, which);
+  } else {
+    // one group at a time: every kernel launch covers one subgraph
+    RsbOpts o1 = o;
+    o1.use_graphs = 0;
+    DBuf<double> f_one((size_t)N);
+    for (size_t q = 0; q < ast.size(); q++) {
+      std::vector<GState> res;
+      std::vector<ll> s1 = {ast[q]}, n1 = {an[q]};
+      run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_one.p, res);
+      CK(cudaMemcpyAsync(f_pos.p + ast[q], f_one.p + ast[q], an[q] * sizeof(double),
+                         cudaMemcpyDeviceToDevice, st));
+      collect(res, std::vector<int>{(int)q});
+    }
+  }
+  k_scatter_f<<<grid_for(N, 256), 256, 0, st>>>(perm.p, f_pos.p, N, d_f);
+  CK_LAUNCH();
+  sync();
+}
+
+void fiedler_groups_device(const long long *d_vtx, ll N, int nv, const int *d_group_of,
+                           int ngroups, const RsbOpts &o, double *d_f, long long *iters,
+                           double *resid) {
   if (o.miter > MAX_MITER || o.miter < 1)
     throw ArgError{PARRSB_ERR_UNSUPPORTED, "rsb_max_iter outside [1, 120]"};
   if (o.fp32)
-    rsb_impl<float>(d_vtx, cent, N, nv, P, o, d_part);
+    fiedler_groups_impl<float>(d_vtx, N, nv, d_group_of, ngroups, o, d_f, iters, resid);
   else
-    rsb_impl<double>(d_vtx, cent, N, nv, P, o, d_part);
+    fiedler_groups_impl<double>(d_vtx, N, nv, d_group_of, ngroups, o, d_f, iters, resid);
+}
+
+void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv, int P,
+                const RsbOpts &o, int *d_part, int *d_seq) {
+  if (o.miter > MAX_MITER || o.miter < 1)
+    throw ArgError{PARRSB_ERR_UNSUPPORTED, "rsb_max_iter outside [1, 120]"};
+  if (o.fp32)
+    rsb_impl<float>(d_vtx, cent, N, nv, P, o, d_part, d_seq);
+  else
+    rsb_impl<double>(d_vtx, cent, N, nv, P, o, d_part, d_seq);
 }
 
 }  // namespace prsb

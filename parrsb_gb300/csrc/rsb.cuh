@@ -27,16 +27,18 @@ struct RsbOpts {
   int check_resid = 1;  // FP64 eigen-residual of every Fiedler vector
   int profile = 0;
   int use_graphs = 1;   // capture each Lanczos pass in a CUDA graph
+  int batched = 1;      // all groups of a level per launch (0: one group at a time)
 };
 
 // Partition N elements (vertex ids d_vtx, centroids cent) into P parts.
 void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv,
-                int P, const RsbOpts &o, int *d_part);
+                int P, const RsbOpts &o, int *d_part, int *d_seq = nullptr);
 
 // Fiedler vectors of independent element groups: group g is the elements
-// e with group_of[e] == g (groups listed in element order).  Used by the
-// batched level solve; f receives the normalised Fiedler vector per element
-// and iters (host, ngroups) the Lanczos steps of each group.
+// e with group_of[e] == g, taken in element order (that order defines the
+// start vector, as the current order does inside RSB).  f receives the
+// normalised Fiedler vector per element (0 for groups of one element);
+// iters / resid (host, ngroups) the Lanczos steps and FP64 eigen-residual.
 void fiedler_groups_device(const long long *d_vtx, ll N, int nv,
                            const int *d_group_of, int ngroups,
                            const RsbOpts &o, double *d_f, long long *iters,

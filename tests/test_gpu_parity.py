@@ -170,3 +170,43 @@ def test_rsb_repeatable(oracle):
     a = P.part_mesh(vtx, xyz, 8, partitioner=0)
     b = P.part_mesh(vtx, xyz, 8, partitioner=0)
     np.testing.assert_array_equal(a, b)
+
+
+# ------------------------------------------- order (seq) and large segments
+def _oracle_seq(order, part, nparts):
+    seq = np.empty(len(part), np.int32)
+    first = {}
+    for i, e in enumerate(order):
+        first.setdefault(part[e], i)
+        seq[e] = i - first[part[e]]
+    return seq
+
+
+@pytest.mark.parametrize("partitioner", [1, 2])
+@pytest.mark.parametrize("shape,nparts", [((16, 16, 16), 8), ((40, 36, 20), 7),
+                                          ((48, 40, 20), 1024), ((9, 7, 5), 3)])
+def test_bisection_seq_bit_exact(oracle, partitioner, shape, nparts):
+    vtx, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=nparts)
+    part, seq = P.part_mesh_seq(vtx, xyz, nparts, partitioner=partitioner)
+    rc, ref, order, _, _ = oracle.part_mesh(vtx, xyz, nparts, partitioner=partitioner,
+                                            want_order=True)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
+    np.testing.assert_array_equal(seq, _oracle_seq(order, ref, nparts))
+
+
+def test_rcb_unjittered_ties_bit_exact(oracle):
+    """Massive key ties (no jitter): the stable tie-break must agree."""
+    vtx, xyz = meshgen.box_hex(24, 20, 18, jitter=0.0)
+    part, seq = P.part_mesh_seq(vtx, xyz, 13, partitioner=1)
+    rc, ref, order, _, _ = oracle.part_mesh(vtx, xyz, 13, partitioner=1, want_order=True)
+    np.testing.assert_array_equal(part, ref)
+    np.testing.assert_array_equal(seq, _oracle_seq(order, ref, 13))
+
+
+def test_rsb_larger_groups(oracle):
+    """Groups larger than one CTA's shared-memory sort (global levels first)."""
+    vtx, xyz = meshgen.box_hex(40, 32, 20, jitter=0.1, seed=8)
+    part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, 4)
+    np.testing.assert_array_equal(sizes, rs)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
