@@ -94,6 +94,19 @@ PARRSB_API void fparrsb_conn_mesh(long long *vtx, double *coord, int *nel, int *
                        long long *periodicInfo, int *nPeriodicFaces,
                        double *tol, int *err);
 
+/* Mesh files (src/parRSB.h:75-83, src/io.c), read and written by one host
+ * process instead of MPI-IO.  parrsb_read_mesh reads <name>.re2 (read & 1:
+ * corner coordinates in preprocessor order, periodic faces as (eid, fid, e1,
+ * e2)) and/or <name>.co2 (read & 2: vertex ids); outputs are malloc'ed and
+ * owned by the caller.  parrsb_dump_con writes <name>.co2.  parrsb_dump_map
+ * writes <name>.ma2; it takes the part array explicitly because there is no
+ * per-rank element distribution to take it from. */
+PARRSB_API int parrsb_read_mesh(unsigned *nel, unsigned *nv, long long **vl, double **coord,
+                                unsigned *nbcs, long long **bcs, char *name, int read);
+PARRSB_API int parrsb_dump_con(char *name, unsigned nelt, unsigned nv, long long *vl);
+PARRSB_API int parrsb_dump_map(char *name, unsigned nelt, unsigned nv, long long *vtx,
+                               const int *part);
+
 /* ------------------------------------------------------------------------
  * Extensions (no counterpart in the reference).
  * ---------------------------------------------------------------------- */

@@ -28,7 +28,8 @@ LIB_PATH = os.path.join(HERE, "libparrsb_gb300.so")
 EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
            "fparrsb_conn_mesh", "parrsb_part_mesh_device",
            "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
-           "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq"]
+           "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq",
+           "parrsb_read_mesh", "parrsb_dump_con", "parrsb_dump_map"]
 
 
 class ParrsbError(RuntimeError):
@@ -102,6 +103,9 @@ def library(build_if_missing=False):
     L.parrsb_fiedler_groups.argtypes = [P, P, P, P, P, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_int, ctypes.POINTER(ParrsbOptions),
                                         ctypes.c_int]
+    L.parrsb_read_mesh.argtypes = [P, P, P, P, P, P, ctypes.c_char_p, ctypes.c_int]
+    L.parrsb_dump_con.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_uint, P]
+    L.parrsb_dump_map.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_uint, P, P]
     L.parrsb_gpu_finalize.argtypes = []
     L.parrsb_gpu_finalize.restype = None
     _lib = L
@@ -210,6 +214,81 @@ def fiedler_groups(vtx, group, ngroups, batched=True, **kw):
     return f, it, rs
 
 
+_libc = None
+
+
+def _free(ptr):
+    global _libc
+    if _libc is None:
+        _libc = ctypes.CDLL(None)
+        _libc.free.argtypes = [ctypes.c_void_p]
+    _libc.free(ptr)
+
+
+def read_mesh(name, read=1):
+    """parrsb_read_mesh: returns dict with 'coord' (nel, nv, ndim) and
+    'periodic' (nbcs, 4) for read & 1, 'vtx' (nel, nv) for read & 2."""
+    nel, nv, nb = ctypes.c_uint(0), ctypes.c_uint(0), ctypes.c_uint(0)
+    vl, co, bc = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    rc = library().parrsb_read_mesh(ctypes.byref(nel), ctypes.byref(nv), ctypes.byref(vl),
+                                    ctypes.byref(co), ctypes.byref(nb), ctypes.byref(bc),
+                                    name.encode(), read)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_read_mesh")
+    out = {}
+    n, v = nel.value, nv.value
+    nd = 3 if v == 8 else 2
+    if read & 1:
+        a = np.ctypeslib.as_array(ctypes.cast(co, ctypes.POINTER(ctypes.c_double)),
+                                  shape=(max(n * v * nd, 1),))
+        out["coord"] = a[:n * v * nd].reshape(n, v, nd).copy()
+        b = np.ctypeslib.as_array(ctypes.cast(bc, ctypes.POINTER(ctypes.c_longlong)),
+                                  shape=(max(4 * nb.value, 1),))
+        out["periodic"] = b[:4 * nb.value].reshape(nb.value, 4).copy()
+        _free(co)
+        _free(bc)
+    if read & 2:
+        a = np.ctypeslib.as_array(ctypes.cast(vl, ctypes.POINTER(ctypes.c_longlong)),
+                                  shape=(max(n * v, 1),))
+        out["vtx"] = a[:n * v].reshape(n, v).copy()
+        _free(vl)
+    return out
+
+
+def dump_con(name, vtx):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    rc = library().parrsb_dump_con(name.encode(), len(vtx), vtx.shape[1], _ptr(vtx))
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_dump_con")
+
+
+def dump_map(name, vtx, part):
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    part = np.ascontiguousarray(part, np.int32)
+    rc = library().parrsb_dump_map(name.encode(), len(vtx), vtx.shape[1], _ptr(vtx), _ptr(part))
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_dump_map")
+
+
+def write_re2(name, coord, periodic=()):
+    """Write a Nek5000 .re2 file (the layout parrsb_read_mesh reads) from
+    corner coordinates (nel, nv, ndim) in preprocessor order."""
+    coord = np.asarray(coord, np.float64)
+    nel, nv, nd = coord.shape
+    with open(name + ".re2", "wb") as f:
+        hdr = f"#v003 {nel:10d} {nd:2d} {nel:10d} synthetic".ljust(80)
+        f.write(hdr.encode()[:80])
+        f.write(np.float32(6.54321).tobytes())
+        rec = np.zeros((nel, 1 + nv * nd))
+        rec[:, 1:] = coord.transpose(0, 2, 1).reshape(nel, nv * nd)
+        f.write(rec.tobytes())
+        f.write(np.float64(0.0).tobytes())  # no curves
+        f.write(np.float64(len(periodic)).tobytes())
+        for eid, fid, e1, e2 in periodic:
+            f.write(np.array([eid, fid, e1, e2, 0, 0, 0], np.float64).tobytes())
+            f.write(b"P       ")
+
+
 def last_stats():
     s = Stats()
     library().parrsb_get_stats(ctypes.byref(s))
@@ -221,7 +300,8 @@ def finalize():
         _lib.parrsb_gpu_finalize()
 
 
-__all__ = ["part_mesh", "part_mesh_seq", "conn_mesh", "part_quality", "last_stats", "fiedler_groups",
+__all__ = ["part_mesh", "part_mesh_seq", "conn_mesh", "read_mesh", "dump_con",
+           "dump_map", "write_re2", "part_quality", "last_stats", "fiedler_groups",
            "default_options", "ParrsbOptions", "ParrsbError", "DEFAULTS",
            "library", "finalize", "OK", "ERR_ARGS", "ERR_CUDA", "ERR_CHECK",
            "ERR_UNSUPPORTED"]
