@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--fp32", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the per-group (unbatched) comparison step")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the RCB / RIB / gencon legs")
     return ap.parse_args()
 
 
@@ -191,6 +195,64 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def _time_device(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    best = None
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        best = t if best is None else min(best, t)
+    return best
+
+
+def other_rows(P, meshgen, lib, torch, ctypes):
+    """RCB / RIB of the 512x512 quad annulus (262,144 elements) to 1024 parts,
+    gencon on the same annulus (the reference algorithm's element check
+    fails there) and on a 128x128x64 jittered hex box (8.4M corner points);
+    device-resident inputs, best of 3 after a warm-up."""
+    from parrsb_gb300.options import ParrsbOptions
+    out = {}
+    vtx, xyz = meshgen.annulus_quad(512, 512, amp=0.02, seed=0)
+    d_xyz = torch.from_numpy(xyz).cuda()
+    d_part = torch.empty(len(xyz), dtype=torch.int32, device="cuda")
+    for name, pa in (("rcb", 1), ("rib", 2)):
+        def run(pa=pa):
+            o = ParrsbOptions.make(partitioner=pa, verbose_level=0)
+            rc = lib.parrsb_part_mesh_device(ctypes.c_void_p(d_part.data_ptr()), None,
+                                             ctypes.c_void_p(d_xyz.data_ptr()), len(xyz), 4,
+                                             ctypes.byref(o), 1024)
+            assert rc == 0
+        t = _time_device(run)
+        out[name + "_annulus_512x512_to_1024"] = {"s": t, "elements_per_s": len(xyz) / t}
+    d_ids = torch.empty(xyz.shape[0] * 4, dtype=torch.int64, device="cuda")
+
+    def gc2():
+        rc = lib.parrsb_conn_mesh_device(ctypes.c_void_p(d_ids.data_ptr()),
+                                         ctypes.c_void_p(d_xyz.data_ptr()), len(xyz), 2, 0.2)
+        assert rc == 1  # element_check fails, as in the reference algorithm
+    t = _time_device(gc2)
+    out["gencon_annulus_512x512"] = {"s": t, "return_code": 1,
+                                     "distinct_ids": int(P.last_stats().gencon_segments)}
+    _, xyz3 = meshgen.box_hex(128, 128, 64, jitter=0.1, seed=0)
+    d3 = torch.from_numpy(xyz3).cuda()
+    ids3 = torch.empty(xyz3.shape[0] * 8, dtype=torch.int64, device="cuda")
+
+    def gc3():
+        rc = lib.parrsb_conn_mesh_device(ctypes.c_void_p(ids3.data_ptr()),
+                                         ctypes.c_void_p(d3.data_ptr()), len(xyz3), 3, 0.2)
+        assert rc == 0
+    t = _time_device(gc3)
+    out["gencon_hex_box_128x128x64"] = {"s": t, "points_per_s": xyz3.shape[0] * 8 / t,
+                                        "distinct_ids": int(P.last_stats().gencon_segments)}
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -287,6 +349,23 @@ def main():
     else:
         part = d_part.cpu().numpy()
     q = P.part_quality(part, vtx, nparts)
+    # ---- plain GPU path: every group of a level solved by its own launches
+    plain = None
+    if not args.no_plain:
+        os.environ["PARRSB_GPU_BATCHED"] = "0"
+        barrier()
+        tp0 = time.perf_counter()
+        sp = step_device()
+        barrier()
+        plain = {"value": max_over_ranks(time.perf_counter() - tp0), "unit": "s",
+                 "what": "one step with per-group Lanczos launches (no batching, no graphs)",
+                 "lanczos_steps": int(sp.lanczos_iters),
+                 "kernel_launches": int(sp.kernel_launches)}
+        os.environ["PARRSB_GPU_BATCHED"] = "1"
+
+    extras = None
+    if not args.no_extras and rank == 0:
+        extras = other_rows(P, meshgen, lib, torch, ctypes)
 
     s = stats[-1]
     spmv_ms = sum(x.spmv_ms for x in stats)
@@ -332,6 +411,8 @@ def main():
                      "spmv_ms_per_launch": spmv_ms / spmv_launches if spmv_launches else None,
                      "algorithmic_bytes_per_launch": per_launch_bytes},
         "cpu_baseline": cpu,
+        "plain_gpu": plain,
+        "other_rows": extras,
         "clocks": clock_info,
         "gpu_launches": int(sum(x.kernel_launches for x in stats)),
         "elements_per_s": nel / t_dev,

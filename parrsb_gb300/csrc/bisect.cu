@@ -43,6 +43,36 @@ __device__ __forceinline__ bool seg_active(int p, ll n, int do_local) {
   return p > 1 || (do_local && p == 1 && n >= 2);
 }
 
+// Bounding boxes are reduced on order-preserving integer keys (integer
+// min / max instead of the low-throughput FP64 pipe); the key's bits travel
+// in the double arrays of the tree.
+__device__ __forceinline__ double key_bits(double x) {
+  return __longlong_as_double((long long)ordered_key(x));
+}
+__device__ __forceinline__ double bits_to_value(double kb) {
+  unsigned long long k = (unsigned long long)__double_as_longlong(kb);
+  unsigned long long b = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
+  return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double warp_min_key(double v) {
+  unsigned long long k = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, k, off);
+    k = o < k ? o : k;
+  }
+  return __longlong_as_double((long long)k);
+}
+__device__ __forceinline__ double warp_max_key(double v) {
+  unsigned long long k = (unsigned long long)__double_as_longlong(v);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, k, off);
+    k = o > k ? o : k;
+  }
+  return __longlong_as_double((long long)k);
+}
+
 __device__ __forceinline__ ll find_seg(const ll *off, ll nseg, ll w) {
   ll lo = 0, hi = nseg - 1;  // last s with off[s] <= w
   while (lo < hi) {
@@ -79,8 +109,8 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
   double v[V];
 #pragma unroll
   for (int q = 0; q < V; q++) {
-    if (BBOX)
-      v[q] = q < 3 ? DBL_MAX : -DBL_MAX;
+    if (BBOX)  // identities of min / max on ordered keys
+      v[q] = __longlong_as_double(q < 3 ? (long long)~0ull : 0ll);
     else
       v[q] = 0.0;
   }
@@ -93,8 +123,8 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
       int e = perm[seg_start[s] + i];
       double c0 = cent[e], c1 = cent[N + e], c2 = cent[2 * N + e];
       if (GEN == GEN_BBOX) {
-        v[0] = c0, v[1] = c1, v[2] = c2;
-        v[3] = c0, v[4] = c1, v[5] = c2;
+        v[0] = key_bits(c0), v[1] = key_bits(c1), v[2] = key_bits(c2);
+        v[3] = v[0], v[4] = v[1], v[5] = v[2];
       } else if (GEN == GEN_MEAN) {
         v[0] = c0, v[1] = c1;
         if (V > 2) v[V - 1] = c2;
@@ -122,7 +152,7 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
     if (copy_only)
       r = v[q];
     else if (BBOX)
-      r = q < 3 ? warp_min(v[q]) : warp_max(v[q]);
+      r = q < 3 ? warp_min_key(v[q]) : warp_max_key(v[q]);
     else
       r = warp_tree_sum(v[q]);
     if (lane == 0) out[w * V + q] = r;
@@ -142,7 +172,8 @@ __global__ void k_rcb_axis(const double *__restrict__ bbox, const int *__restric
   if (s >= nseg) return;
   const double *b = bbox + 6 * s;
   double len[3];
-  for (int d = 0; d < ndim; d++) len[d] = __dsub_rn(b[3 + d], b[d]);
+  for (int d = 0; d < ndim; d++)
+    len[d] = __dsub_rn(bits_to_value(b[3 + d]), bits_to_value(b[d]));
   int ax = 0;
   for (int d = 1; d < ndim; d++)
     if (len[d] > len[ax]) ax = d;

@@ -243,6 +243,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.fp32 = env_int("PARRSB_GPU_FP32", 0);
     ro.check_resid = env_int("PARRSB_GPU_CHECK_RESID", 1);
     ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
+    ro.batched = env_int("PARRSB_GPU_BATCHED", 1);
     rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq);
     sync();
   } else {

@@ -669,6 +669,174 @@ __device__ __forceinline__ double sign_of(double a, double b) {
   return b >= 0.0 ? fabs(a) : -fabs(a);
 }
 
+// Tridiagonal eigensolve for the Ritz vector, one thread per group.
+// The eigenvalues come from the reference's implicit-QL iteration (tqli,
+// src/fiedler.c:328-432, same arithmetic) run without accumulating the
+// eigenvector matrix; only four rows of the rotation product are carried
+// (O(1) per rotation instead of O(n)).  The eigenvector of the eigenvalue of
+// least modulus is then obtained by inverse iteration on the original T
+// (LU with partial pivoting, two solves) and its sign is chosen so that it
+// agrees with the rotation product on the largest carried component --
+// i.e. the orientation tqli's accumulated eigenvector would have.  If QL
+// exceeds 30 sweeps (tqli's failure return) the partially converged values
+// are used the same way.  Writes coef[j] = y_j / |r_j|.
+constexpr int EIG_ROWS = 4;
+
+__device__ void tri_solve_pivot(int n, const double *a0, const double *e, double lam,
+                                double *x, double *a, double *b, double *c, double *c2,
+                                int *piv, double tiny) {
+  // factor (T - lam I) = P L U with U having two super-diagonals (dgttrf)
+  for (int i = 0; i < n; i++) a[i] = __dsub_rn(a0[i], lam);
+  for (int i = 0; i < n - 1; i++) b[i] = e[i], c[i] = e[i], c2[i] = 0.0;
+  for (int i = 0; i < n - 1; i++) {
+    if (fabs(a[i]) >= fabs(b[i])) {
+      piv[i] = 0;
+      if (a[i] == 0.0) a[i] = tiny;
+      double fact = __ddiv_rn(b[i], a[i]);
+      b[i] = fact;
+      a[i + 1] = __dsub_rn(a[i + 1], __dmul_rn(fact, c[i]));
+      c2[i] = 0.0;
+    } else {
+      piv[i] = 1;
+      double fact = __ddiv_rn(a[i], b[i]);
+      a[i] = b[i];
+      b[i] = fact;
+      double t = c[i];
+      c[i] = a[i + 1];
+      a[i + 1] = __dsub_rn(t, __dmul_rn(fact, a[i + 1]));
+      if (i < n - 2) {
+        c2[i] = c[i + 1];
+        c[i + 1] = __dmul_rn(-fact, c[i + 1]);
+      } else {
+        c2[i] = 0.0;
+      }
+    }
+  }
+  if (n > 0 && a[n - 1] == 0.0) a[n - 1] = tiny;
+  // forward: L with row interchanges
+  for (int i = 0; i < n - 1; i++) {
+    if (piv[i]) {
+      double t = x[i];
+      x[i] = x[i + 1];
+      x[i + 1] = __dsub_rn(t, __dmul_rn(b[i], x[i]));
+    } else {
+      x[i + 1] = __dsub_rn(x[i + 1], __dmul_rn(b[i], x[i]));
+    }
+  }
+  // backward: U
+  for (int i = n - 1; i >= 0; i--) {
+    double v = x[i];
+    if (i + 1 < n) v = __dsub_rn(v, __dmul_rn(c[i], x[i + 1]));
+    if (i + 2 < n) v = __dsub_rn(v, __dmul_rn(c2[i], x[i + 2]));
+    x[i] = __ddiv_rn(v, a[i]);
+  }
+}
+
+__global__ void k_tri_eig(GState *__restrict__ gs, int ngroups,
+                          const double *__restrict__ diagT, const double *__restrict__ upperT,
+                          const double *__restrict__ vnorm, int MI, double *__restrict__ coef,
+                          double *__restrict__ scratch) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  GState &st = gs[g];
+  if (!st.active) return;
+  const int n = st.iters;
+  // per-thread scratch: d, e, Q rows, a, b, c, c2, x  (MI each) + piv
+  double *d = scratch + (ll)g * (12 + EIG_ROWS) * MI;
+  double *e = d + MI;
+  double *q = e + MI;  // EIG_ROWS rows of length MI
+  double *a = q + EIG_ROWS * MI, *b = a + MI, *c = b + MI, *c2 = c + MI, *x = c2 + MI;
+  int *piv = (int *)(x + MI);
+  const double *D0 = diagT + (ll)g * MI, *E0 = upperT + (ll)g * MI;
+  for (int i = 0; i < n; i++) d[i] = D0[i];
+  for (int i = 0; i < n - 1; i++) e[i] = E0[i];
+  if (n > 0) e[n - 1] = 0.0;
+  const int nr = n < EIG_ROWS ? n : EIG_ROWS;
+  for (int r = 0; r < nr; r++)
+    for (int j = 0; j < n; j++) q[r * MI + j] = (r == j) ? 1.0 : 0.0;
+  for (int l = 0; l < n; l++) {
+    int iter = 0, m;
+    bool fail = false;
+    do {
+      for (m = l; m < n - 1; m++) {
+        double dd = __dadd_rn(fabs(d[m]), fabs(d[m + 1]));
+        if (__ddiv_rn(fabs(e[m]), dd) < 1e-12) break;
+      }
+      if (m != l) {
+        if (iter++ == 30) {
+          fail = true;
+          break;
+        }
+        double gg = __ddiv_rn(__dsub_rn(d[l + 1], d[l]), __dmul_rn(2.0, e[l]));
+        double r = __dsqrt_rn(__dadd_rn(__dmul_rn(gg, gg), 1.0));
+        double sg = gg >= 0.0 ? fabs(r) : -fabs(r);
+        gg = __dadd_rn(__dsub_rn(d[m], d[l]), __ddiv_rn(e[l], __dadd_rn(gg, sg)));
+        double s = 1.0, cc = 1.0, p = 0.0;
+        int i;
+        for (i = m - 1; i >= l; i--) {
+          double f = __dmul_rn(s, e[i]);
+          double bb = __dmul_rn(cc, e[i]);
+          if (fabs(f) >= fabs(gg)) {
+            cc = __ddiv_rn(gg, f);
+            r = __dsqrt_rn(__dadd_rn(__dmul_rn(cc, cc), 1.0));
+            e[i + 1] = __dmul_rn(f, r);
+            s = __ddiv_rn(1.0, r);
+            cc = __dmul_rn(cc, s);
+          } else {
+            s = __ddiv_rn(f, gg);
+            r = __dsqrt_rn(__dadd_rn(__dmul_rn(s, s), 1.0));
+            e[i + 1] = __dmul_rn(gg, r);
+            cc = __ddiv_rn(1.0, r);
+            s = __dmul_rn(s, cc);
+          }
+          gg = __dsub_rn(d[i + 1], p);
+          r = __dadd_rn(__dmul_rn(__dsub_rn(d[i], gg), s), __dmul_rn(__dmul_rn(2.0, cc), bb));
+          p = __dmul_rn(s, r);
+          d[i + 1] = __dadd_rn(gg, p);
+          gg = __dsub_rn(__dmul_rn(cc, r), bb);
+          for (int k = 0; k < nr; k++) {  // carried rows of the rotation product
+            double f2 = q[k * MI + i + 1];
+            q[k * MI + i + 1] = __dadd_rn(__dmul_rn(s, q[k * MI + i]), __dmul_rn(cc, f2));
+            q[k * MI + i] = __dsub_rn(__dmul_rn(cc, q[k * MI + i]), __dmul_rn(s, f2));
+          }
+        }
+        if (r < 1e-12 && i >= l) continue;
+        d[l] = __dsub_rn(d[l], p);
+        e[l] = gg;
+        e[m] = 0.0;
+      }
+    } while (m != l);
+    if (fail) break;
+  }
+  int mi = 0;
+  double emin = fabs(d[0]);
+  for (int i = 1; i < n; i++)
+    if (fabs(d[i]) < emin) emin = fabs(d[i]), mi = i;
+  double lam = d[mi];
+  // inverse iteration on the original T
+  double tnorm = 0.0;
+  for (int i = 0; i < n; i++)
+    tnorm = fmax(tnorm, fabs(D0[i]) + (i > 0 ? fabs(E0[i - 1]) : 0.0) + (i < n - 1 ? fabs(E0[i]) : 0.0));
+  double tiny = fmax(tnorm, 1e-300) * 1e-16;
+  for (int i = 0; i < n; i++) x[i] = 1.0;
+  for (int sweep = 0; sweep < 2; sweep++) {
+    tri_solve_pivot(n, D0, E0, lam, x, a, b, c, c2, piv, tiny);
+    double nrm = 0.0;
+    for (int i = 0; i < n; i++) nrm = __dadd_rn(nrm, __dmul_rn(x[i], x[i]));
+    nrm = __dsqrt_rn(nrm);
+    double inv = nrm > 0.0 ? __ddiv_rn(1.0, nrm) : 0.0;
+    for (int i = 0; i < n; i++) x[i] = __dmul_rn(x[i], inv);
+  }
+  // orientation of tqli's eigenvector: its components in the carried rows
+  int rb = 0;
+  for (int r = 1; r < nr; r++)
+    if (fabs(q[r * MI + mi]) > fabs(q[rb * MI + mi])) rb = r;
+  double ref = nr > 0 ? q[rb * MI + mi] : 1.0;
+  double sgn = ((ref >= 0.0) == (x[rb] >= 0.0)) ? 1.0 : -1.0;
+  for (int j = 0; j < n; j++)
+    coef[(ll)g * MI + j] = __ddiv_rn(__dmul_rn(sgn, x[j]), vnorm[(ll)g * (MI + 1) + j]);
+}
+
 // Implicit-QL tridiagonal eigensolve of one group's T (the reference's tqli,
 // src/fiedler.c:328-432) by one warp: the scalar recurrences run redundantly
 // on every lane, the eigenvector rotations are split over the lanes.  Writes
@@ -811,7 +979,7 @@ struct Lanczos {
   DBuf<ll> tbeg, tend;
   DBuf<int> tgrp;
   DBuf<VT> f, r, p, w, V;
-  DBuf<double> part, diagT, upperT, vnorm, coef, y64;
+  DBuf<double> part, diagT, upperT, vnorm, coef, y64, eigs;
   DBuf<int> any;  // [0] any group active for another pass, [1] max steps
   DBuf<int> cnt;  // per-group arrival counters of the fused finalisation
   std::vector<GState> hgs;
@@ -854,6 +1022,7 @@ struct Lanczos {
     any.ensure(2);
     cnt.ensure(A);
     CK(cudaMemsetAsync(cnt.p, 0, (size_t)A * sizeof(int), ctx().stream));
+    eigs.ensure((size_t)A * (12 + EIG_ROWS) * MI);
   }
 
   FinArgs fargs(int it, double tol, int mpass) {
@@ -914,8 +1083,8 @@ struct Lanczos {
       (*spmv_launches)++;
       tile<TM_R, GATE_RUN, FIN_RTR>(it, nullptr, tol, mpass);
     }
-    size_t smem = ((size_t)MI * MI + 2 * MI) * sizeof(double);
-    k_tqli<<<A, 32, smem, st>>>(gs.p, A, diagT.p, upperT.p, vnorm.p, MI, coef.p);
+    k_tri_eig<<<grid_for(A, 32), 32, 0, st>>>(gs.p, A, diagT.p, upperT.p, vnorm.p, MI,
+                                                coef.p, eigs.p);
     CK_LAUNCH();
     k_ritz<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, V.p, N, coef.p, MI,
                                          f.p, part.p);
@@ -973,9 +1142,6 @@ struct Lanczos {
     // the vectors are scratch until the first pass initialises them
     CK(cudaMemsetAsync(p.p, 0, (size_t)N * sizeof(VT), st));
     autotune(lv);
-    size_t smem = ((size_t)MI * MI + 2 * MI) * sizeof(double);
-    if (smem > 48 * 1024)
-      CK(cudaFuncSetAttribute(k_tqli, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
     CK_LAUNCH();
     if (!warm) initial_vector();
@@ -1441,7 +1607,21 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     }
     // ---- Fiedler vectors (src/rsb.c:300-302)
     std::vector<GState> res;
-    run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res);
+    if (o.batched) {
+      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res);
+    } else {
+      // plain path: every group of the level solved by its own launches
+      RsbOpts o1 = o;
+      o1.use_graphs = 0;
+      for (int g = 0; g < na; g++) {
+        std::vector<GState> r1;
+        std::vector<ll> s1 = {ast[g]}, n1 = {an[g]};
+        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1);
+        CK(cudaMemcpyAsync(f_pos.p + ast[g], f_tmp.p + ast[g], an[g] * sizeof(double),
+                           cudaMemcpyDeviceToDevice, st));
+        res.push_back(r1[0]);
+      }
+    }
     ll rows = 0;
     for (int g = 0; g < na; g++) {
       S.lanczos_iters += res[g].total_iters;

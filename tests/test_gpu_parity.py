@@ -210,3 +210,13 @@ def test_rsb_larger_groups(oracle):
     part, ref, sizes, rs, q, qr, st, info = _rsb_compare(oracle, vtx, xyz, 4)
     np.testing.assert_array_equal(sizes, rs)
     assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+
+
+def test_rsb_plain_equals_batched(monkeypatch):
+    """Per-group launches (the plain path) give bitwise the batched result:
+    group reductions do not depend on the other groups of the level."""
+    vtx, xyz = meshgen.box_hex(12, 10, 8, jitter=0.1, seed=3)
+    a = P.part_mesh(vtx, xyz, 6, partitioner=0)
+    monkeypatch.setenv("PARRSB_GPU_BATCHED", "0")
+    b = P.part_mesh(vtx, xyz, 6, partitioner=0)
+    np.testing.assert_array_equal(a, b)
