@@ -145,6 +145,9 @@ typedef struct {
   int unconverged;            /* bisections that used all restarts */
   long long nnz;              /* off-diagonal nonzeros of the dual graph */
   long long gencon_segments;  /* gencon: number of distinct ids */
+  double lanczos_ms[6];       /* timing mode: p update, r update, eigensolve,
+                                 Ritz vector, pass set-up, host per pass */
+  long long lanczos_passes;   /* graph launches (Lanczos restarts of a level) */
 } parrsb_stats;
 
 enum {

@@ -650,6 +650,14 @@ static int fiedler_group(double *f, const csr_t *L, int miter, int mpass,
   for (ll i = 0; i < n; i++) norm += f[i] * f[i];
   double normi = 1.0 / sqrt(norm);
   for (ll i = 0; i < n; i++) f[i] *= normi;
+  /* Canonical orientation (shared with the GPU): the reference's sign comes
+   * from tqli's accumulated rotations; here f is oriented like the step of
+   * the start vector, sum_i f_i s_i >= 0 with s_i = +1 for i < n/2 and -1
+   * otherwise.  A flip swaps the two halves of the bisection. */
+  double orient = 0.0;
+  for (ll i = 0; i < n; i++) orient += (i < n / 2) ? f[i] : -f[i];
+  if (orient < 0.0)
+    for (ll i = 0; i < n; i++) f[i] = -f[i];
   free(initv);
   return iter;
 }

@@ -12,7 +12,10 @@
  *   - every sort is stable in the current element order;
  *   - RIB's means and inertia sums use tree_sum (32-wide tiles, shuffle-down
  *     tree, repeated until one value);
- *   - RIB's power iteration starts from (31, 17, 43)/50 instead of rand().
+ *   - RIB's power iteration starts from (31, 17, 43)/50 instead of rand();
+ *   - a Fiedler vector is oriented so that sum_i f_i s_i >= 0, s_i = +1 on
+ *     the first half of the group's order and -1 on the second (the
+ *     reference's sign is whatever tqli's rotations give).
  * Parity against the real reference is UNPINNED: the reference needs MPI and
  * gslib (neither exists here) and ships no golden outputs for this path.
  */

@@ -52,13 +52,15 @@ class Stats(ctypes.Structure):
                 ("max_fiedler_resid", ctypes.c_double),
                 ("unconverged", ctypes.c_int),
                 ("nnz", ctypes.c_longlong),
-                ("gencon_segments", ctypes.c_longlong)]
+                ("gencon_segments", ctypes.c_longlong),
+                ("lanczos_ms", ctypes.c_double * 6),
+                ("lanczos_passes", ctypes.c_longlong)]
 
     def as_dict(self):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            d[name] = list(v) if name == "stage_ms" else v
+            d[name] = list(v) if name in ("stage_ms", "lanczos_ms") else v
         return d
 
 

@@ -32,7 +32,11 @@ namespace prsb {
 namespace {
 
 constexpr int LZ_THREADS = 256;
-constexpr ll LZ_TILE = 2048;
+constexpr ll LZ_TILE = 2048;  // largest tile (rows); smaller groups use 512
+
+// Rows per tile of a group of n rows: big groups keep few partials per
+// reduction, smaller ones get enough blocks to fill the GPU.
+inline ll tile_rows(ll n) { return n >= (1ll << 20) ? LZ_TILE : 512; }
 constexpr int MAX_MITER = 120;
 
 // ----------------------------------------------------------------------------
@@ -238,7 +242,8 @@ enum FinOp {
   FIN_PASS_END,
   FIN_NORM,
   FIN_RESID1,
-  FIN_RESID2
+  FIN_RESID2,
+  FIN_ORIENT
 };
 
 // One block per group: reduce the group's tile partials in a fixed order and
@@ -322,6 +327,8 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     s.c = __ddiv_rn(tot[0], tot[1]);  // Rayleigh quotient
   } else if (OP == FIN_RESID2) {
     s.resid = __ddiv_rn(__dsqrt_rn(tot[0]), __dsqrt_rn(s.ff));
+  } else if (OP == FIN_ORIENT) {
+    if (tot[0] < 0.0) s.c = -s.c;  // canonical sign: sum_i s_i f_i >= 0
   }
 }
 
@@ -386,7 +393,8 @@ enum TileMode {
   TM_SCALE_F = 9,    // f *= c
   TM_RESID1 = 10,    // y = L f in FP64 -> y64; sums f.y, f.f
   TM_RESID2 = 11,    // sum (y - rho f)^2
-  TM_SUM_F_WARM = 12 // same as TM_SUM_F but for a warm start vector
+  TM_SUM_F_WARM = 12, // same as TM_SUM_F but for a warm start vector
+  TM_ORIENT = 13      // sum s_i f_i, s = +1 on the first half of the group, -1 after
 };
 
 // Canonical per-tile reductions.  A tile's rows are cut into 32-row chunks
@@ -492,6 +500,8 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         f[i] = f[i] - c;
       } else if (MODE == TM_SQ_F) {
         tv.set_prod(f[i], f[i]);
+      } else if (MODE == TM_ORIENT) {
+        tv.set((i - s.start) < s.n / 2 ? f[i] : -f[i]);
       } else if (MODE == TM_SCALE_F) {
         f[i] = (VT)((double)f[i] * s.c);
       } else if (MODE == TM_RESID1) {
@@ -665,22 +675,57 @@ k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
 }
 
-__device__ __forceinline__ double sign_of(double a, double b) {
-  return b >= 0.0 ? fabs(a) : -fabs(a);
+
+// Tridiagonal eigensolve for the Ritz vector, one warp per group.
+// GB300 runs long dependent FP64 chains slowly, so instead of the implicit
+// QL sweep of the reference (tqli, src/fiedler.c:328-432, about 2000
+// dependent rotations with divisions and square roots for n = 50):
+//   1. the eigenvalue of least modulus (the one lanczos picks,
+//      src/fiedler.c:538-545) by warp multisection: 32 lanes evaluate a
+//      division-free Sturm count at 32 shifts per round, the bracket
+//      shrinks 33x per round;
+//   2. its eigenvector by inverse iteration on T (LU with partial
+//      pivoting, two solves, Newton reciprocals), normalised.
+// The vector's sign is fixed later, on the final Fiedler vector (canonical
+// orientation).  Writes coef[j] = y_j / |r_j|.
+
+// number of eigenvalues of T below x (Sturm sequence of the leading
+// principal minors, rescaled by powers of two to stay in range)
+__device__ __forceinline__ int sturm_count(const double *d, const double *e2, int n, double x) {
+  double pm = 1.0, p = __dsub_rn(d[0], x);
+  int cnt = 0;
+  if (p == 0.0) p = -1e-300;
+  if (p < 0.0) cnt++;
+  for (int i = 1; i < n; i++) {
+    double pn = fma(__dsub_rn(d[i], x), p, -__dmul_rn(e2[i - 1], pm));
+    if (pn == 0.0) pn = (p > 0.0) ? -1e-300 : 1e-300;  // sign opposite to p
+    if ((pn < 0.0) != (p < 0.0)) cnt++;
+    pm = p;
+    p = pn;
+    double ap = fabs(p);
+    if (ap > 1e200) {
+      p = __dmul_rn(p, 1e-200), pm = __dmul_rn(pm, 1e-200);
+    } else if (ap < 1e-200) {
+      p = __dmul_rn(p, 1e200), pm = __dmul_rn(pm, 1e200);
+    }
+  }
+  return cnt;
 }
 
-// Tridiagonal eigensolve for the Ritz vector, one thread per group.
-// The eigenvalues come from the reference's implicit-QL iteration (tqli,
-// src/fiedler.c:328-432, same arithmetic) run without accumulating the
-// eigenvector matrix; only four rows of the rotation product are carried
-// (O(1) per rotation instead of O(n)).  The eigenvector of the eigenvalue of
-// least modulus is then obtained by inverse iteration on the original T
-// (LU with partial pivoting, two solves) and its sign is chosen so that it
-// agrees with the rotation product on the largest carried component --
-// i.e. the orientation tqli's accumulated eigenvector would have.  If QL
-// exceeds 30 sweeps (tqli's failure return) the partially converged values
-// are used the same way.  Writes coef[j] = y_j / |r_j|.
-constexpr int EIG_ROWS = 4;
+// y / x with a single-precision reciprocal refined by two Newton steps
+__device__ __forceinline__ double fast_div(double y, double x) {
+  double ax = fabs(x);
+  double r;
+  if (ax > 1e-30 && ax < 1e30) {
+    r = (double)__frcp_rn((float)x);
+    r = fma(r, fma(-x, r, 1.0), r);
+    r = fma(r, fma(-x, r, 1.0), r);
+  } else {
+    r = __ddiv_rn(1.0, x);
+  }
+  double q = __dmul_rn(y, r);
+  return fma(r, fma(-x, q, y), q);  // one correction of the quotient
+}
 
 __device__ void tri_solve_pivot(int n, const double *a0, const double *e, double lam,
                                 double *x, double *a, double *b, double *c, double *c2,
@@ -692,18 +737,18 @@ __device__ void tri_solve_pivot(int n, const double *a0, const double *e, double
     if (fabs(a[i]) >= fabs(b[i])) {
       piv[i] = 0;
       if (a[i] == 0.0) a[i] = tiny;
-      double fact = __ddiv_rn(b[i], a[i]);
+      double fact = fast_div(b[i], a[i]);
       b[i] = fact;
-      a[i + 1] = __dsub_rn(a[i + 1], __dmul_rn(fact, c[i]));
+      a[i + 1] = fma(-fact, c[i], a[i + 1]);
       c2[i] = 0.0;
     } else {
       piv[i] = 1;
-      double fact = __ddiv_rn(a[i], b[i]);
+      double fact = fast_div(a[i], b[i]);
       a[i] = b[i];
       b[i] = fact;
       double t = c[i];
       c[i] = a[i + 1];
-      a[i + 1] = __dsub_rn(t, __dmul_rn(fact, a[i + 1]));
+      a[i + 1] = fma(-fact, a[i + 1], t);
       if (i < n - 2) {
         c2[i] = c[i + 1];
         c[i + 1] = __dmul_rn(-fact, c[i + 1]);
@@ -713,239 +758,116 @@ __device__ void tri_solve_pivot(int n, const double *a0, const double *e, double
     }
   }
   if (n > 0 && a[n - 1] == 0.0) a[n - 1] = tiny;
-  // forward: L with row interchanges
-  for (int i = 0; i < n - 1; i++) {
+  for (int i = 0; i < n - 1; i++) {  // L with row interchanges
     if (piv[i]) {
       double t = x[i];
       x[i] = x[i + 1];
-      x[i + 1] = __dsub_rn(t, __dmul_rn(b[i], x[i]));
+      x[i + 1] = fma(-b[i], x[i], t);
     } else {
-      x[i + 1] = __dsub_rn(x[i + 1], __dmul_rn(b[i], x[i]));
+      x[i + 1] = fma(-b[i], x[i], x[i + 1]);
     }
   }
-  // backward: U
-  for (int i = n - 1; i >= 0; i--) {
+  for (int i = n - 1; i >= 0; i--) {  // U
     double v = x[i];
-    if (i + 1 < n) v = __dsub_rn(v, __dmul_rn(c[i], x[i + 1]));
-    if (i + 2 < n) v = __dsub_rn(v, __dmul_rn(c2[i], x[i + 2]));
-    x[i] = __ddiv_rn(v, a[i]);
+    if (i + 1 < n) v = fma(-c[i], x[i + 1], v);
+    if (i + 2 < n) v = fma(-c2[i], x[i + 2], v);
+    x[i] = fast_div(v, a[i]);
   }
+}
+
+__device__ __forceinline__ double warp_min_d(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
+
+// k-th smallest eigenvalue (0-based) by multisection inside [lo, hi]
+__device__ double eig_index(const double *d, const double *e2, int n, int k, double lo,
+                            double hi) {
+  const int lane = threadIdx.x;
+  double a = lo, b = hi;
+  for (int round = 0; round < 24; round++) {
+    double w = __dsub_rn(b, a);
+    if (!(w > 2.2e-16 * fmax(fabs(a), fabs(b)) + 1e-300)) break;
+    double x = fma(w, (double)(lane + 1) / 33.0, a);
+    int cnt = sturm_count(d, e2, n, x);
+    unsigned ball = __ballot_sync(0xffffffffu, cnt > k);
+    int first = ball ? __ffs(ball) - 1 : 32;
+    double xl = __shfl_sync(0xffffffffu, x, first > 0 ? first - 1 : 0);
+    double xr = __shfl_sync(0xffffffffu, x, first < 32 ? first : 31);
+    double na = first > 0 ? xl : a;
+    double nb = first < 32 ? xr : b;
+    if (!(nb < b || na > a)) break;  // no progress at this precision
+    a = na, b = nb;
+  }
+  return 0.5 * (a + b);
 }
 
 __global__ void k_tri_eig(GState *__restrict__ gs, int ngroups,
                           const double *__restrict__ diagT, const double *__restrict__ upperT,
-                          const double *__restrict__ vnorm, int MI, double *__restrict__ coef,
-                          double *__restrict__ scratch) {
-  int g = blockIdx.x * blockDim.x + threadIdx.x;
+                          const double *__restrict__ vnorm, int MI, double *__restrict__ coef) {
+  extern __shared__ double eig_sm[];
+  const int g = blockIdx.x, lane = threadIdx.x;
   if (g >= ngroups) return;
   GState &st = gs[g];
   if (!st.active) return;
   const int n = st.iters;
-  // per-thread scratch: d, e, Q rows, a, b, c, c2, x  (MI each) + piv
-  double *d = scratch + (ll)g * (12 + EIG_ROWS) * MI;
-  double *e = d + MI;
-  double *q = e + MI;  // EIG_ROWS rows of length MI
-  double *a = q + EIG_ROWS * MI, *b = a + MI, *c = b + MI, *c2 = c + MI, *x = c2 + MI;
+  double *D0 = eig_sm, *E0 = D0 + MI, *e2 = E0 + MI;
+  double *a = e2 + MI, *b = a + MI, *c = b + MI, *c2 = c + MI, *x = c2 + MI;
   int *piv = (int *)(x + MI);
-  const double *D0 = diagT + (ll)g * MI, *E0 = upperT + (ll)g * MI;
-  for (int i = 0; i < n; i++) d[i] = D0[i];
-  for (int i = 0; i < n - 1; i++) e[i] = E0[i];
-  if (n > 0) e[n - 1] = 0.0;
-  const int nr = n < EIG_ROWS ? n : EIG_ROWS;
-  for (int r = 0; r < nr; r++)
-    for (int j = 0; j < n; j++) q[r * MI + j] = (r == j) ? 1.0 : 0.0;
-  for (int l = 0; l < n; l++) {
-    int iter = 0, m;
-    bool fail = false;
-    do {
-      for (m = l; m < n - 1; m++) {
-        double dd = __dadd_rn(fabs(d[m]), fabs(d[m + 1]));
-        if (__ddiv_rn(fabs(e[m]), dd) < 1e-12) break;
-      }
-      if (m != l) {
-        if (iter++ == 30) {
-          fail = true;
-          break;
-        }
-        double gg = __ddiv_rn(__dsub_rn(d[l + 1], d[l]), __dmul_rn(2.0, e[l]));
-        double r = __dsqrt_rn(__dadd_rn(__dmul_rn(gg, gg), 1.0));
-        double sg = gg >= 0.0 ? fabs(r) : -fabs(r);
-        gg = __dadd_rn(__dsub_rn(d[m], d[l]), __ddiv_rn(e[l], __dadd_rn(gg, sg)));
-        double s = 1.0, cc = 1.0, p = 0.0;
-        int i;
-        for (i = m - 1; i >= l; i--) {
-          double f = __dmul_rn(s, e[i]);
-          double bb = __dmul_rn(cc, e[i]);
-          if (fabs(f) >= fabs(gg)) {
-            cc = __ddiv_rn(gg, f);
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(cc, cc), 1.0));
-            e[i + 1] = __dmul_rn(f, r);
-            s = __ddiv_rn(1.0, r);
-            cc = __dmul_rn(cc, s);
-          } else {
-            s = __ddiv_rn(f, gg);
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(s, s), 1.0));
-            e[i + 1] = __dmul_rn(gg, r);
-            cc = __ddiv_rn(1.0, r);
-            s = __dmul_rn(s, cc);
-          }
-          gg = __dsub_rn(d[i + 1], p);
-          r = __dadd_rn(__dmul_rn(__dsub_rn(d[i], gg), s), __dmul_rn(__dmul_rn(2.0, cc), bb));
-          p = __dmul_rn(s, r);
-          d[i + 1] = __dadd_rn(gg, p);
-          gg = __dsub_rn(__dmul_rn(cc, r), bb);
-          for (int k = 0; k < nr; k++) {  // carried rows of the rotation product
-            double f2 = q[k * MI + i + 1];
-            q[k * MI + i + 1] = __dadd_rn(__dmul_rn(s, q[k * MI + i]), __dmul_rn(cc, f2));
-            q[k * MI + i] = __dsub_rn(__dmul_rn(cc, q[k * MI + i]), __dmul_rn(s, f2));
-          }
-        }
-        if (r < 1e-12 && i >= l) continue;
-        d[l] = __dsub_rn(d[l], p);
-        e[l] = gg;
-        e[m] = 0.0;
-      }
-    } while (m != l);
-    if (fail) break;
+  for (int i = lane; i < n; i += 32) {
+    D0[i] = diagT[(ll)g * MI + i];
+    if (i < n - 1) {
+      double ev = upperT[(ll)g * MI + i];
+      E0[i] = ev;
+      e2[i] = __dmul_rn(ev, ev);
+    }
   }
-  int mi = 0;
-  double emin = fabs(d[0]);
-  for (int i = 1; i < n; i++)
-    if (fabs(d[i]) < emin) emin = fabs(d[i]), mi = i;
-  double lam = d[mi];
-  // inverse iteration on the original T
-  double tnorm = 0.0;
-  for (int i = 0; i < n; i++)
-    tnorm = fmax(tnorm, fabs(D0[i]) + (i > 0 ? fabs(E0[i - 1]) : 0.0) + (i < n - 1 ? fabs(E0[i]) : 0.0));
-  double tiny = fmax(tnorm, 1e-300) * 1e-16;
-  for (int i = 0; i < n; i++) x[i] = 1.0;
-  for (int sweep = 0; sweep < 2; sweep++) {
-    tri_solve_pivot(n, D0, E0, lam, x, a, b, c, c2, piv, tiny);
-    double nrm = 0.0;
-    for (int i = 0; i < n; i++) nrm = __dadd_rn(nrm, __dmul_rn(x[i], x[i]));
-    nrm = __dsqrt_rn(nrm);
-    double inv = nrm > 0.0 ? __ddiv_rn(1.0, nrm) : 0.0;
-    for (int i = 0; i < n; i++) x[i] = __dmul_rn(x[i], inv);
+  __syncwarp();
+  // Gershgorin interval
+  double glo = 1e300, ghi = -1e300;
+  for (int i = lane; i < n; i += 32) {
+    double r = (i > 0 ? fabs(E0[i - 1]) : 0.0) + (i < n - 1 ? fabs(E0[i]) : 0.0);
+    glo = fmin(glo, __dsub_rn(D0[i], r));
+    ghi = fmax(ghi, __dadd_rn(D0[i], r));
   }
-  // orientation of tqli's eigenvector: its components in the carried rows
-  int rb = 0;
-  for (int r = 1; r < nr; r++)
-    if (fabs(q[r * MI + mi]) > fabs(q[rb * MI + mi])) rb = r;
-  double ref = nr > 0 ? q[rb * MI + mi] : 1.0;
-  double sgn = ((ref >= 0.0) == (x[rb] >= 0.0)) ? 1.0 : -1.0;
-  for (int j = 0; j < n; j++)
-    coef[(ll)g * MI + j] = __ddiv_rn(__dmul_rn(sgn, x[j]), vnorm[(ll)g * (MI + 1) + j]);
-}
-
-// Implicit-QL tridiagonal eigensolve of one group's T (the reference's tqli,
-// src/fiedler.c:328-432) by one warp: the scalar recurrences run redundantly
-// on every lane, the eigenvector rotations are split over the lanes.  Writes
-// coef[j] = y_j / |r_j|, y = eigenvector of the eigenvalue of least modulus.
-__global__ void k_tqli(GState *__restrict__ gs, int ngroups,
-                       const double *__restrict__ diagT,
-                       const double *__restrict__ upperT,
-                       const double *__restrict__ vnorm, int MI,
-                       double *__restrict__ coef) {
-  extern __shared__ double sm[];
-  int g = blockIdx.x;
-  if (g >= ngroups) return;
-  GState &st = gs[g];
-  if (!st.active) return;
-  int n = st.iters;
-  int lane = threadIdx.x;
-  double *E = sm;
-  double *d = E + (ll)MI * MI;
-  double *e = d + MI;
-  for (int idx = lane; idx < n * n; idx += 32) E[idx] = (idx / n == idx % n) ? 1.0 : 0.0;
+  glo = warp_min_d(glo);
+  ghi = warp_max_d(ghi);
+  double pad = fmax(1e-300, 2.2e-16 * fmax(fabs(glo), fabs(ghi))) * 4.0;
+  glo -= pad, ghi += pad;
+  // eigenvalue of least modulus: the negative one closest to 0 or the
+  // smallest non-negative one
+  int c0 = sturm_count(D0, e2, n, 0.0);  // eigenvalues below 0 (all lanes agree)
+  double lam;
+  if (c0 == 0) {
+    lam = eig_index(D0, e2, n, 0, glo, ghi);
+  } else if (c0 >= n) {
+    lam = eig_index(D0, e2, n, n - 1, glo, ghi);
+  } else {
+    double ln = eig_index(D0, e2, n, c0 - 1, glo, ghi);
+    double lp = eig_index(D0, e2, n, c0, glo, ghi);
+    lam = fabs(lp) < fabs(ln) ? lp : ln;
+  }
   if (lane == 0) {
-    for (int i = 0; i < n; i++) d[i] = diagT[(ll)g * MI + i];
-    for (int i = 0; i < n - 1; i++) e[i] = upperT[(ll)g * MI + i];
-    if (n > 0) e[n - 1] = 0.0;
+    double tnorm = fmax(fabs(glo), fabs(ghi));
+    double tiny = fmax(tnorm, 1e-300) * 1e-16;
+    for (int i = 0; i < n; i++) x[i] = 1.0;
+    for (int sweep = 0; sweep < 2; sweep++) {
+      tri_solve_pivot(n, D0, E0, lam, x, a, b, c, c2, piv, tiny);
+      double nrm = 0.0;
+      for (int i = 0; i < n; i++) nrm = fma(x[i], x[i], nrm);
+      double inv = nrm > 0.0 ? fast_div(1.0, __dsqrt_rn(nrm)) : 0.0;
+      for (int i = 0; i < n; i++) x[i] = __dmul_rn(x[i], inv);
+    }
   }
   __syncwarp();
-  int fail = 0;
-  for (int l = 0; l < n && !fail; l++) {
-    int iter = 0, m;
-    do {
-      for (m = l; m < n - 1; m++) {
-        double dd = __dadd_rn(fabs(d[m]), fabs(d[m + 1]));
-        if (__ddiv_rn(fabs(e[m]), dd) < 1e-12) break;
-      }
-      if (m != l) {
-        if (iter++ == 30) {
-          fail = 1;
-          break;
-        }
-        double gg = __ddiv_rn(__dsub_rn(d[l + 1], d[l]), __dmul_rn(2.0, e[l]));
-        double r = __dsqrt_rn(__dadd_rn(__dmul_rn(gg, gg), 1.0));
-        gg = __dadd_rn(__dsub_rn(d[m], d[l]), __ddiv_rn(e[l], __dadd_rn(gg, sign_of(r, gg))));
-        double s = 1.0, c = 1.0, p = 0.0;
-        int i;
-        for (i = m - 1; i >= l; i--) {
-          double f = __dmul_rn(s, e[i]);
-          double b = __dmul_rn(c, e[i]);
-          double enew;
-          if (fabs(f) >= fabs(gg)) {
-            c = __ddiv_rn(gg, f);
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(c, c), 1.0));
-            enew = __dmul_rn(f, r);
-            s = __ddiv_rn(1.0, r);
-            c = __dmul_rn(c, s);
-          } else {
-            s = __ddiv_rn(f, gg);
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(s, s), 1.0));
-            enew = __dmul_rn(gg, r);
-            c = __ddiv_rn(1.0, r);
-            s = __dmul_rn(s, c);
-          }
-          gg = __dsub_rn(d[i + 1], p);
-          r = __dadd_rn(__dmul_rn(__dsub_rn(d[i], gg), s), __dmul_rn(__dmul_rn(2.0, c), b));
-          p = __dmul_rn(s, r);
-          double dnew = __dadd_rn(gg, p);
-          gg = __dsub_rn(__dmul_rn(c, r), b);
-          __syncwarp();
-          if (lane == 0) {
-            e[i + 1] = enew;
-            d[i + 1] = dnew;
-          }
-          for (int k = lane; k < n; k += 32) {
-            double f2 = E[k * n + i + 1];
-            E[k * n + i + 1] = __dadd_rn(__dmul_rn(s, E[k * n + i]), __dmul_rn(c, f2));
-            E[k * n + i] = __dsub_rn(__dmul_rn(c, E[k * n + i]), __dmul_rn(s, f2));
-          }
-          __syncwarp();
-        }
-        if (r < 1e-12 && i >= l) continue;
-        __syncwarp();
-        if (lane == 0) {
-          d[l] = __dsub_rn(d[l], p);
-          e[l] = gg;
-          e[m] = 0.0;
-        }
-        __syncwarp();
-      }
-    } while (m != l);
-  }
-  __syncwarp();
-  // eigenvalue of least modulus (first minimum)
-  int mi = 0;
-  double emin = fabs(d[0]);
-  for (int i = 1; i < n; i++)
-    if (fabs(d[i]) < emin) emin = fabs(d[i]), mi = i;
-  double scale = 1.0;
-  if (!fail) {
-    double acc = 0.0;
-    for (int k = lane; k < n; k += 32) acc = __dadd_rn(acc, __dmul_rn(E[k * n + mi], E[k * n + mi]));
-    acc = warp_tree_sum(acc);
-    acc = __shfl_sync(0xffffffffu, acc, 0);
-    double nrm = acc;
-    if (nrm > 0.0) nrm = __dsqrt_rn(fabs(nrm));
-    scale = __ddiv_rn(1.0, nrm);
-  }
-  for (int j = lane; j < n; j += 32) {
-    double yj = fail ? E[mi * n + j] : __dmul_rn(E[j * n + mi], scale);
-    coef[(ll)g * MI + j] = __ddiv_rn(yj, vnorm[(ll)g * (MI + 1) + j]);
-  }
+  for (int j = lane; j < n; j += 32)
+    coef[(ll)g * MI + j] = fast_div(x[j], vnorm[(ll)g * (MI + 1) + j]);
 }
 
 __global__ void k_set_active(GState *__restrict__ gs, int ngroups) {
@@ -979,11 +901,12 @@ struct Lanczos {
   DBuf<ll> tbeg, tend;
   DBuf<int> tgrp;
   DBuf<VT> f, r, p, w, V;
-  DBuf<double> part, diagT, upperT, vnorm, coef, y64, eigs;
+  DBuf<double> part, diagT, upperT, vnorm, coef, y64;
   DBuf<int> any;  // [0] any group active for another pass, [1] max steps
   DBuf<int> cnt;  // per-group arrival counters of the fused finalisation
   std::vector<GState> hgs;
   std::vector<cudaEvent_t> ev;  // SpMV start/stop events (timing mode)
+  std::vector<cudaEvent_t> evk; // p / r per step, then init, eig, ritz (timing mode)
   int bd = 256;                  // threads per tile block (autotuned per level)
 
   void setup(const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N_, int miter) {
@@ -1000,9 +923,12 @@ struct Lanczos {
       s.n = gn[g];
       s.miter = (int)std::min<ll>(miter, gn[g]);
       s.tile0 = (int)hb.size();
-      for (ll b = gstart[g]; b < gstart[g] + gn[g]; b += LZ_TILE) {
+      // tile rows depend only on the group's size (never on the other groups
+      // of the level), so batched and one-group-at-a-time runs agree bitwise
+      const ll tr = tile_rows(gn[g]);
+      for (ll b = gstart[g]; b < gstart[g] + gn[g]; b += tr) {
         hb.push_back(b);
-        he.push_back(std::min(b + LZ_TILE, gstart[g] + gn[g]));
+        he.push_back(std::min(b + tr, gstart[g] + gn[g]));
         hg.push_back(g);
       }
       s.ntiles = (int)hb.size() - s.tile0;
@@ -1022,7 +948,12 @@ struct Lanczos {
     any.ensure(2);
     cnt.ensure(A);
     CK(cudaMemsetAsync(cnt.p, 0, (size_t)A * sizeof(int), ctx().stream));
-    eigs.ensure((size_t)A * (12 + EIG_ROWS) * MI);
+
+  }
+
+  // shared memory of k_tri_eig: 8 arrays of MI doubles and MI ints
+  size_t eig_smem() const {
+    return (size_t)8 * MI * sizeof(double) + (size_t)(MI + 2) * sizeof(int) + 16;
   }
 
   FinArgs fargs(int it, double tol, int mpass) {
@@ -1064,16 +995,26 @@ struct Lanczos {
 
   // One Lanczos pass (restart) for the active groups: the body that the
   // CUDA graph captures.
+  void mark(int k) {
+    if (!evk.empty())
+      CK(cudaEventRecordWithFlags(evk[k], ctx().stream, cudaEventRecordExternal));
+  }
+  // evk layout: [4 it .. 4 it + 3] p start/stop, r start/stop of step it;
+  // then 4 MI + 0..5: init start/stop, eig start/stop, ritz start/stop
   void pass_body(const Level &lv, double tol, int mpass, long long *spmv_launches) {
     cudaStream_t st = ctx().stream;
+    mark(4 * MI + 0);
     tile<TM_SUM_F, GATE_ACTIVE>();
     fin<FIN_INIT_MEAN, GATE_ACTIVE>();
     tile<TM_INIT_R, GATE_ACTIVE>();
     fin<FIN_INIT_RTR, GATE_ACTIVE>(0, tol);
+    mark(4 * MI + 1);
     for (int it = 0; it < MI; it++) {
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
+      mark(4 * it + 0);
       tile<TM_P, GATE_RUN, FIN_PMEAN>(it, nullptr, tol, mpass);
+      mark(4 * it + 1);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
       k_spmv<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
                                    lv.slice_w.p, p.p, w.p, part.p, fargs(it, tol, mpass), 1,
@@ -1081,14 +1022,19 @@ struct Lanczos {
       CK_LAUNCH();
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
+      mark(4 * it + 2);
       tile<TM_R, GATE_RUN, FIN_RTR>(it, nullptr, tol, mpass);
+      mark(4 * it + 3);
     }
-    k_tri_eig<<<grid_for(A, 32), 32, 0, st>>>(gs.p, A, diagT.p, upperT.p, vnorm.p, MI,
-                                                coef.p, eigs.p);
+    mark(4 * MI + 2);
+    k_tri_eig<<<A, 32, eig_smem(), st>>>(gs.p, A, diagT.p, upperT.p, vnorm.p, MI, coef.p);
     CK_LAUNCH();
+    mark(4 * MI + 3);
+    mark(4 * MI + 4);
     k_ritz<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, V.p, N, coef.p, MI,
                                          f.p, part.p);
     CK_LAUNCH();
+    mark(4 * MI + 5);
     fin<FIN_RITZ_MEAN, GATE_ACTIVE>();
     tile<TM_SUB_C, GATE_ACTIVE>();
     fin<FIN_PASS_END, GATE_ACTIVE>(0, tol, mpass);
@@ -1141,6 +1087,9 @@ struct Lanczos {
     cudaStream_t st = ctx().stream;
     // the vectors are scratch until the first pass initialises them
     CK(cudaMemsetAsync(p.p, 0, (size_t)N * sizeof(VT), st));
+    if (eig_smem() > 48 * 1024)
+      CK(cudaFuncSetAttribute(k_tri_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)eig_smem()));
     autotune(lv);
     k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
     CK_LAUNCH();
@@ -1151,6 +1100,8 @@ struct Lanczos {
     if (ctx().timing) {
       ev.assign(2 * MI, nullptr);
       for (auto &e : ev) CK(cudaEventCreate(&e));
+      evk.assign(4 * MI + 6, nullptr);
+      for (auto &e : evk) CK(cudaEventCreate(&e));
     }
     if (use_graph) {
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -1175,23 +1126,40 @@ struct Lanczos {
       d2h(h_any, any.p, 2);
       sync();
       launches += h_any[1];  // SpMV launches that did work this pass
+      ctx().stats.lanczos_passes++;
       if (!ev.empty()) {
-        for (int it = 0; it < h_any[1]; it++) {
+        auto el = [&](cudaEvent_t a, cudaEvent_t b) {
           float ms = 0.f;
-          CK(cudaEventElapsedTime(&ms, ev[2 * it], ev[2 * it + 1]));
-          ctx().stats.spmv_ms += ms;
+          CK(cudaEventElapsedTime(&ms, a, b));
+          return (double)ms;
+        };
+        double *lm = ctx().stats.lanczos_ms;
+        for (int it = 0; it < MI; it++) {
+          if (it < h_any[1]) ctx().stats.spmv_ms += el(ev[2 * it], ev[2 * it + 1]);
+          lm[0] += el(evk[4 * it + 0], evk[4 * it + 1]);
+          lm[1] += el(evk[4 * it + 2], evk[4 * it + 3]);
         }
+        lm[4] += el(evk[4 * MI + 0], evk[4 * MI + 1]);
+        lm[2] += el(evk[4 * MI + 2], evk[4 * MI + 3]);
+        lm[3] += el(evk[4 * MI + 4], evk[4 * MI + 5]);
+        // wall time of the whole pass on the device minus its parts
+        lm[5] += el(evk[4 * MI + 0], evk[4 * MI + 5]);
       }
       if (!h_any[0]) break;
     }
     for (auto &e : ev) cudaEventDestroy(e);
     ev.clear();
+    for (auto &e : evk) cudaEventDestroy(e);
+    evk.clear();
     ctx().stats.spmv_launches += launches;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    // normalise (src/fiedler.c:606-613)
+    // normalise (src/fiedler.c:606-613), then fix the sign canonically:
+    // sum_i s_i f_i >= 0 with s = +1 on the first half of the group's order
     tile<TM_SQ_F, GATE_ALL>();
     fin<FIN_NORM, GATE_ALL>();
+    tile<TM_ORIENT, GATE_ALL>();
+    fin<FIN_ORIENT, GATE_ALL>();
     tile<TM_SCALE_F, GATE_ALL>();
   }
 
