@@ -386,8 +386,8 @@ enum TileMode {
   TM_IV_WRITE = 2,   // f = (initv - c) * scale   (scale in alpha)
   TM_SUM_F = 3,      // sum f
   TM_INIT_R = 4,     // r = f - c, V0 = r, sum r^2
-  TM_P = 5,          // p = beta (p - c) + r, sum p
-  TM_R = 6,          // r -= alpha w, V[it+1] = r, sum r^2
+  TM_P = 5,          // k_pr: p = beta (p - c) + r, sum p      (r = V[it])
+  TM_R = 6,          // k_pr: V[it+1] = V[it] - alpha w, sum V[it+1]^2
   TM_SUB_C = 7,      // f -= c
   TM_SQ_F = 8,       // sum f^2
   TM_SCALE_F = 9,    // f *= c
@@ -448,7 +448,6 @@ template <typename VT, int MODE, int GATE, int FUSE>
 __global__ void __launch_bounds__(512)
 k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        const int *__restrict__ tgrp, GState *__restrict__ gs, VT *__restrict__ f,
-       VT *__restrict__ r, VT *__restrict__ p, const VT *__restrict__ w,
        VT *__restrict__ V, ll N, int it, double *__restrict__ part,
        const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
        const int *__restrict__ slice_w, double *__restrict__ y64, FinArgs fa) {
@@ -458,7 +457,7 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   int g = tgrp[t];
   const GState &s = gs[g];
   if (!gate_ok(s, GATE)) return;
-  const VT c = (VT)s.c, beta = (VT)s.beta, alpha = (VT)s.alpha;
+  const VT c = (VT)s.c;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const ll b = tbeg[t], e = tend[t];
   const ll c0 = b >> 5;
@@ -484,17 +483,7 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         tv.set(f[i]);
       } else if (MODE == TM_INIT_R) {
         VT qv = f[i] - c;
-        r[i] = qv;
-        V[i] = qv;
-        tv.set_prod(qv, qv);
-      } else if (MODE == TM_P) {
-        VT qv = it == 0 ? r[i] : (VT)fma(beta, p[i] - c, r[i]);
-        p[i] = qv;
-        tv.set(qv);
-      } else if (MODE == TM_R) {
-        VT qv = (VT)fma(-alpha, w[i], r[i]);
-        r[i] = qv;
-        V[(ll)(it + 1) * N + i] = qv;
+        V[i] = qv;  // r_0 is row 0 of the Krylov basis
         tv.set_prod(qv, qv);
       } else if (MODE == TM_SUB_C) {
         f[i] = f[i] - c;
@@ -546,12 +535,160 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   }
 }
 
+// Rows per lane of the vectorised tile kernels: one 16-byte load per array.
+template <typename VT>
+struct VecOf;
+template <>
+struct VecOf<float> {
+  using T = float4;
+  static constexpr int R = 4;
+  __device__ static __forceinline__ void get(const T &v, float *x) {
+    x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
+  }
+  __device__ static __forceinline__ T make(const float *x) {
+    return make_float4(x[0], x[1], x[2], x[3]);
+  }
+};
+template <>
+struct VecOf<double> {
+  using T = double2;
+  static constexpr int R = 2;
+  __device__ static __forceinline__ void get(const T &v, double *x) { x[0] = v.x, x[1] = v.y; }
+  __device__ static __forceinline__ T make(const double *x) { return make_double2(x[0], x[1]); }
+};
+
+// rows [i0, i0 + R) of a, restricted to the tile [b, e) (others read as 0)
+template <typename VT>
+__device__ __forceinline__ void load_rows(const VT *__restrict__ a, ll i0, ll b, ll e,
+                                          VT *x) {
+  using V = VecOf<VT>;
+  if (i0 >= b && i0 + V::R <= e) {
+    V::get(*reinterpret_cast<const typename V::T *>(a + i0), x);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V::R; k++) x[k] = (i0 + k >= b && i0 + k < e) ? a[i0 + k] : (VT)0;
+  }
+}
+template <typename VT>
+__device__ __forceinline__ void store_rows(VT *__restrict__ a, ll i0, ll b, ll e,
+                                           const VT *x) {
+  using V = VecOf<VT>;
+  if (i0 >= b && i0 + V::R <= e) {
+    *reinterpret_cast<typename V::T *>(a + i0) = V::make(x);
+  } else {
+#pragma unroll
+    for (int k = 0; k < V::R; k++)
+      if (i0 + k >= b && i0 + k < e) a[i0 + k] = x[k];
+  }
+}
+
+// A lane's running sum of its rows' terms: compensated pair in FP32, plain
+// FP64 otherwise; chunk() reduces the warp's pairs with the fixed tree.
+template <typename VT>
+struct LaneSum {
+  VT s = (VT)0, c = (VT)0;
+  __device__ __forceinline__ void add(const Term<VT> &t);
+  __device__ __forceinline__ double chunk() const;
+};
+template <>
+__device__ __forceinline__ void LaneSum<float>::add(const Term<float> &t) {
+  two_sum_pair(s, c, t.s, t.c);
+}
+template <>
+__device__ __forceinline__ void LaneSum<double>::add(const Term<double> &t) {
+  s = s + (t.s + t.c);
+}
+template <>
+__device__ __forceinline__ double LaneSum<float>::chunk() const { return chunk_sum_pair(s, c); }
+template <>
+__device__ __forceinline__ double LaneSum<double>::chunk() const { return warp_tree_sum(s); }
+
+// The two vector updates of a Lanczos step (src/fiedler.c:233-262, CG form),
+// R consecutive rows per lane and two chunks of 32 R rows per warp in flight
+// (16-byte loads).  r is row `it` of the Krylov basis V.
+//   TM_P: p = r (it 0) or beta (p - c) + r; tile partial of sum p
+//   TM_R: V[it+1] = V[it] - alpha w; tile partial of sum V[it+1]^2
+// The chunk decomposition (32 R rows, aligned to multiples of 32 R) does not
+// depend on the CTA size.  The last tile block of a group finalises it.
+template <typename VT, int MODE>
+__global__ void __launch_bounds__(512)
+k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+     GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
+     VT *__restrict__ V, ll N, double *__restrict__ part, FinArgs fa) {
+  using Vec = VecOf<VT>;
+  constexpr int R = Vec::R, CH = 32 * R;
+  constexpr int OP = MODE == TM_P ? FIN_PMEAN : FIN_RTR;
+  __shared__ double sh[32];
+  __shared__ double cs[LZ_TILE / CH + 2];
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
+  const GState &s = gs[g];
+  if (!s.run) return;
+  const int it = fa.it;
+  const VT c = (VT)s.c, beta = (VT)s.beta, alpha = (VT)s.alpha;
+  const VT *__restrict__ rv = V + (ll)it * N;
+  VT *__restrict__ rn = V + (ll)(it + 1) * N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const ll b = tbeg[t], e = tend[t];
+  const ll c0 = b / CH;
+  const int nc = (int)((e - 1) / CH - c0 + 1);
+  for (int q0 = 2 * warp; q0 < nc; q0 += 2 * nw) {
+    const bool two = q0 + 1 < nc;  // warp-uniform
+    ll i0[2];
+    VT x[2][R], y[2][R];
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      i0[u] = (c0 + q0 + u) * CH + (ll)lane * R;
+      if (u == 0 || two) {
+        load_rows(rv, i0[u], b, e, x[u]);
+        if (MODE == TM_R || it > 0) load_rows(MODE == TM_P ? (const VT *)p : w, i0[u], b, e, y[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+      if (u == 1 && !two) break;
+      LaneSum<VT> acc;
+      VT o[R];
+#pragma unroll
+      for (int k = 0; k < R; k++) {
+        Term<VT> tv;
+        if (MODE == TM_P) {
+          o[k] = it == 0 ? x[u][k] : (VT)fma(beta, y[u][k] - c, x[u][k]);
+          tv.set(o[k]);
+        } else {
+          o[k] = (VT)fma(-alpha, y[u][k], x[u][k]);
+          tv.set_prod(o[k], o[k]);
+        }
+        if (i0[u] + k >= b && i0[u] + k < e) acc.add(tv);
+      }
+      store_rows(MODE == TM_P ? p : rn, i0[u], b, e, o);
+      double v = acc.chunk();
+      if (lane == 0) cs[q0 + u] = v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
+  fused_fin<OP>(gs, g, part, fa, sh);
+}
+
+// threads per block of k_pr / k_ritz for tiles of at most `rows` rows
+template <typename VT>
+inline int vec_threads(ll rows, int chunks_per_warp) {
+  const ll ch = 32 * VecOf<VT>::R;
+  ll warps = (rows / ch + chunks_per_warp - 1) / chunks_per_warp;
+  if (warps < 1) warps = 1;
+  if (warps > 16) warps = 16;
+  return (int)warps * 32;
+}
+
 // w = L p and sum w_i (p_i - c) per tile.  FP32: difference form
 // w_i = sum_j w_ij (p_i - p_j) with FFMA.  FP64: w_i = d_i p_i - sum_j w_ij p_j
 // (the gather-scatter form of the reference, src/laplacian.c:188-205) with
 // one DFMA per nonzero and the weights taken from a shared-memory table.
 // A warp processes one 32-row ELL slice at a time (fully coalesced index
-// loads, uniform width).
+// loads, uniform width).  The index stream is read with the evict-first
+// policy so that the vectors (p, w, the Krylov rows) stay in L2 between the
+// launches of a step.
 template <typename VT>
 __global__ void __launch_bounds__(512)
 k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
@@ -588,7 +725,7 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
       for (; k + 8 <= wd; k += 8) {
         unsigned x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) x[u] = __ldg(ep + (ll)(k + u) * 32);
+        for (int u = 0; u < 8; u++) x[u] = __ldcs(ep + (ll)(k + u) * 32);
         float pj[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) pj[u] = (float)p[x[u] & 0x0FFFFFFFu];
@@ -596,7 +733,7 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         for (int u = 0; u < 8; u++) sum = fmaf(small_u2f(x[u] >> 28), (float)pi - pj[u], sum);
       }
       for (; k < wd; k++) {
-        unsigned x = __ldg(ep + (ll)k * 32);
+        unsigned x = __ldcs(ep + (ll)k * 32);
         sum = fmaf(small_u2f(x >> 28), (float)pi - (float)p[x & 0x0FFFFFFFu], sum);
       }
       y = (VT)sum;
@@ -608,7 +745,7 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
       for (; k + 8 <= wd; k += 8) {
         unsigned x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) x[u] = __ldg(ep + (ll)(k + u) * 32);
+        for (int u = 0; u < 8; u++) x[u] = __ldcs(ep + (ll)(k + u) * 32);
         double pj[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) pj[u] = (double)p[x[u] & 0x0FFFFFFFu];
@@ -619,7 +756,7 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         }
       }
       for (; k < wd; k++) {
-        unsigned x = __ldg(ep + (ll)k * 32);
+        unsigned x = __ldcs(ep + (ll)k * 32);
         sum = fma(wlut[x >> 28], (double)p[x & 0x0FFFFFFFu], sum);
         dsum += x >> 28;
       }
@@ -638,43 +775,123 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
 }
 
-// f_i = sum_j coef_j V_j[i] (j < iters), sum f per tile (canonical chunks).
+// Ritz vector f_i = sum_j coef_j V_j[i] (j < iters, src/fiedler.c:520-535)
+// and the tile partial of sum f, R rows per lane (16-byte loads of each
+// basis row).  FP32: compensated dot (Ogita, Rump and Oishi's Dot2) with each
+// coefficient split into two floats, so the sum keeps about twice single
+// precision before its one rounding to float.  FP64: DFMA chain.
 template <typename VT>
 __global__ void __launch_bounds__(512)
 k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        const int *__restrict__ tgrp, const GState *__restrict__ gs,
        const VT *__restrict__ V, ll N, const double *__restrict__ coef, int MI,
        VT *__restrict__ f, double *__restrict__ part) {
+  using Vec = VecOf<VT>;
+  constexpr int R = Vec::R, CH = 32 * R;
   __shared__ double cf[MAX_MITER];
-  __shared__ double cs[LZ_TILE / 32 + 1];
-  int t = blockIdx.x;
-  int g = tgrp[t];
+  __shared__ float ch[MAX_MITER], cl[MAX_MITER];
+  __shared__ double cs[LZ_TILE / CH + 2];
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
   const GState &s = gs[g];
   if (!s.active) return;
-  int n = s.iters;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) cf[j] = coef[(ll)g * MI + j];
+  const int n = s.iters;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    double v = coef[(ll)g * MI + j];
+    float hi = __double2float_rn(v);
+    cf[j] = v;
+    ch[j] = hi;
+    cl[j] = __double2float_rn(__dsub_rn(v, (double)hi));
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const ll b = tbeg[t], e = tend[t];
-  const ll c0 = b >> 5;
-  const int nc = (int)(((e - 1) >> 5) - c0 + 1);
+  const ll c0 = b / CH;
+  const int nc = (int)((e - 1) / CH - c0 + 1);
   for (int q = warp; q < nc; q += nw) {
-    ll i = (c0 + q) * 32 + lane;
-    Term<VT> tv;
-    if (i >= b && i < e) {
-      double v = 0.0;
-      for (int j = 0; j < n; j++) v = fma((double)V[(ll)j * N + i], cf[j], v);
-      VT qv = (VT)v;
-      f[i] = qv;
-      tv.set(qv);
+    const ll i0 = (c0 + q) * CH + (ll)lane * R;
+    LaneSum<VT> acc;
+    VT o[R];
+    if (i0 >= b && i0 + R <= e) {
+      // whole vector inside the tile: the j loop over 16-byte loads
+      if (sizeof(VT) == 4) {
+        float sh_[R], sc_[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) sh_[k] = 0.f, sc_[k] = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < n; j++) {
+          VT x[R];
+          Vec::get(*reinterpret_cast<const typename Vec::T *>(V + (ll)j * N + i0), x);
+          const float hj = ch[j], lj = cl[j];
+#pragma unroll
+          for (int k = 0; k < R; k++) {
+            float xv = (float)x[k];
+            float pr = xv * hj;
+            float pe = fmaf(xv, hj, -pr);
+            pe = fmaf(xv, lj, pe);
+            float t1 = sh_[k] + pr;
+            float bp = t1 - sh_[k];
+            float er = (sh_[k] - (t1 - bp)) + (pr - bp);
+            sh_[k] = t1;
+            sc_[k] = sc_[k] + (er + pe);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < R; k++) o[k] = (VT)((double)sh_[k] + (double)sc_[k]);
+      } else {
+        double a_[R];
+#pragma unroll
+        for (int k = 0; k < R; k++) a_[k] = 0.0;
+#pragma unroll 4
+        for (int j = 0; j < n; j++) {
+          VT x[R];
+          Vec::get(*reinterpret_cast<const typename Vec::T *>(V + (ll)j * N + i0), x);
+#pragma unroll
+          for (int k = 0; k < R; k++) a_[k] = fma((double)x[k], cf[j], a_[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < R; k++) o[k] = (VT)a_[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; k++) {
+        const ll i = i0 + k;
+        o[k] = (VT)0;
+        if (i < b || i >= e) continue;
+        if (sizeof(VT) == 4) {
+          float sh1 = 0.f, sc1 = 0.f;
+          for (int j = 0; j < n; j++) {
+            float xv = (float)V[(ll)j * N + i];
+            float pr = xv * ch[j];
+            float pe = fmaf(xv, ch[j], -pr);
+            pe = fmaf(xv, cl[j], pe);
+            float t1 = sh1 + pr;
+            float bp = t1 - sh1;
+            float er = (sh1 - (t1 - bp)) + (pr - bp);
+            sh1 = t1;
+            sc1 = sc1 + (er + pe);
+          }
+          o[k] = (VT)((double)sh1 + (double)sc1);
+        } else {
+          double a1 = 0.0;
+          for (int j = 0; j < n; j++) a1 = fma((double)V[(ll)j * N + i], cf[j], a1);
+          o[k] = (VT)a1;
+        }
+      }
     }
-    double cv = tv.chunk();
-    if (lane == 0) cs[q] = cv;
+#pragma unroll
+    for (int k = 0; k < R; k++) {
+      Term<VT> tv;
+      tv.set(o[k]);
+      if (i0 + k >= b && i0 + k < e) acc.add(tv);
+    }
+    store_rows(f, i0, b, e, o);
+    double v = acc.chunk();
+    if (lane == 0) cs[q] = v;
   }
   __syncthreads();
   if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
 }
-
 
 // Tridiagonal eigensolve for the Ritz vector, one warp per group.
 // GB300 runs long dependent FP64 chains slowly, so instead of the implicit
@@ -900,7 +1117,7 @@ struct Lanczos {
   DBuf<GState> gs;
   DBuf<ll> tbeg, tend;
   DBuf<int> tgrp;
-  DBuf<VT> f, r, p, w, V;
+  DBuf<VT> f, p, w, V;  // Fiedler iterate, CG direction, L p, Krylov basis
   DBuf<double> part, diagT, upperT, vnorm, coef, y64;
   DBuf<int> any;  // [0] any group active for another pass, [1] max steps
   DBuf<int> cnt;  // per-group arrival counters of the fused finalisation
@@ -908,6 +1125,9 @@ struct Lanczos {
   std::vector<cudaEvent_t> ev;  // SpMV start/stop events (timing mode)
   std::vector<cudaEvent_t> evk; // p / r per step, then init, eig, ritz (timing mode)
   int bd = 256;                  // threads per tile block (autotuned per level)
+  int pr_bd = 256;               // threads per block of k_pr
+  int ritz_bd = 256;             // threads per block of k_ritz
+  ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
 
   void setup(const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N_, int miter) {
     N = N_;
@@ -934,14 +1154,19 @@ struct Lanczos {
       s.ntiles = (int)hb.size() - s.tile0;
     }
     T = (int)hb.size();
+    ll max_tile = 0;
+    for (int g = 0; g < A; g++) max_tile = std::max(max_tile, std::min(tile_rows(gn[g]), gn[g]));
+    pr_bd = vec_threads<VT>(max_tile, 2);
+    ritz_bd = vec_threads<VT>(max_tile, 1);
+    VS = (N + 63) & ~(ll)63;
     gs.ensure(A);
     tbeg.ensure(T), tend.ensure(T), tgrp.ensure(T);
     h2d(gs.p, hgs.data(), A);
     h2d(tbeg.p, hb.data(), T);
     h2d(tend.p, he.data(), T);
     h2d(tgrp.p, hg.data(), T);
-    f.ensure(N), r.ensure(N), p.ensure(N), w.ensure(N);
-    V.ensure((size_t)(MI + 1) * N);
+    f.ensure(N), p.ensure(N), w.ensure(N);
+    V.ensure((size_t)(MI + 1) * VS);
     part.ensure((size_t)2 * T + 2);
     diagT.ensure((size_t)A * MI), upperT.ensure((size_t)A * MI);
     vnorm.ensure((size_t)A * (MI + 1)), coef.ensure((size_t)A * MI);
@@ -973,7 +1198,7 @@ struct Lanczos {
   template <int MODE, int GATE, int FUSE = -1>
   void tile(int it = 0, const Level *lv = nullptr, double tol = 0.0, int mpass = 0) {
     k_tile<VT, MODE, GATE, FUSE><<<T, bd, 0, ctx().stream>>>(
-        tbeg.p, tend.p, tgrp.p, gs.p, f.p, r.p, p.p, w.p, V.p, N, it, part.p,
+        tbeg.p, tend.p, tgrp.p, gs.p, f.p, V.p, N, it, part.p,
         lv ? lv->ell.p : nullptr, lv ? lv->slice_off.p : nullptr,
         lv ? lv->slice_w.p : nullptr, y64.p, fargs(it, tol, mpass));
     CK_LAUNCH();
@@ -1013,7 +1238,9 @@ struct Lanczos {
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
       mark(4 * it + 0);
-      tile<TM_P, GATE_RUN, FIN_PMEAN>(it, nullptr, tol, mpass);
+      k_pr<VT, TM_P><<<T, pr_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS,
+                                          part.p, fargs(it, tol, mpass));
+      CK_LAUNCH();
       mark(4 * it + 1);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
       k_spmv<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
@@ -1023,7 +1250,9 @@ struct Lanczos {
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       mark(4 * it + 2);
-      tile<TM_R, GATE_RUN, FIN_RTR>(it, nullptr, tol, mpass);
+      k_pr<VT, TM_R><<<T, pr_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS,
+                                          part.p, fargs(it, tol, mpass));
+      CK_LAUNCH();
       mark(4 * it + 3);
     }
     mark(4 * MI + 2);
@@ -1031,7 +1260,7 @@ struct Lanczos {
     CK_LAUNCH();
     mark(4 * MI + 3);
     mark(4 * MI + 4);
-    k_ritz<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, V.p, N, coef.p, MI,
+    k_ritz<VT><<<T, ritz_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, V.p, VS, coef.p, MI,
                                          f.p, part.p);
     CK_LAUNCH();
     mark(4 * MI + 5);
