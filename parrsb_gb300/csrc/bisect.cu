@@ -287,7 +287,7 @@ __global__ void k_rib_axis(const int *__restrict__ perm,
 
 template <int KIND>
 __global__ void k_keys(const int *__restrict__ perm, const double *__restrict__ cent,
-                       ll N, const int *__restrict__ seg_of_pos,
+                       const u32 *__restrict__ rank, ll N, const int *__restrict__ seg_of_pos,
                        const int *__restrict__ axis_or_act,
                        const double *__restrict__ avg,
                        const double *__restrict__ ev, u64 *__restrict__ keys,
@@ -297,9 +297,9 @@ __global__ void k_keys(const int *__restrict__ perm, const double *__restrict__ 
   int s = seg_of_pos[i];
   int e = perm[i];
   u64 k = 0;
-  if (KIND == BISECT_RCB) {
+  if (KIND == BISECT_RCB) {  // dense rank (order-equivalent to the coordinate)
     int ax = axis_or_act[s];
-    if (ax >= 0) k = ordered_key(cent[(ll)ax * N + e]);
+    if (ax >= 0) k = rank[(ll)ax * N + e];
   } else {
     if (axis_or_act[s]) {
       const double *a = avg + 3 * s, *v = ev + 3 * s;
@@ -361,21 +361,68 @@ __global__ void k_part_from_segs(const int *__restrict__ perm,
 }
 
 // ---------------------------------------------------------------------------
+// Dense coordinate ranks.  RCB only ever compares centroid coordinates along
+// one axis and takes min / max for the bounding boxes, so every coordinate
+// can be replaced by its dense rank among all centroids on that axis (equal
+// values -> equal rank): stable sorts by rank give the same order as stable
+// sorts by value, and a box edge is uniq[max rank] - uniq[min rank], the same
+// difference of the same two doubles.  Ranks are 32-bit keys (fewer radix
+// passes than 64-bit ordered doubles) and are computed once per call.
+// ---------------------------------------------------------------------------
+__global__ void k_axis_keys(const double *__restrict__ cent, ll N, int a,
+                            u64 *__restrict__ keys, int *__restrict__ vals) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  keys[i] = ordered_key(cent[(ll)a * N + i]);
+  vals[i] = (int)i;
+}
+
+__global__ void k_rank_flags(const u64 *__restrict__ keys, ll N, int *__restrict__ flag) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) flag[i] = (i > 0 && keys[i] != keys[i - 1]) ? 1 : 0;
+}
+
+__global__ void k_rank_write(const u64 *__restrict__ keys, const int *__restrict__ vals,
+                             const int *__restrict__ flag, const ll *__restrict__ excl, ll N,
+                             u32 *__restrict__ rank, double *__restrict__ uniq) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  ll r = excl[i] + flag[i];
+  rank[vals[i]] = (u32)r;
+  if (i == 0 || flag[i]) {
+    u64 k = keys[i];
+    u64 bits = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
+    uniq[r] = __longlong_as_double((long long)bits);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Whole-recursion RCB of one small segment per CTA (n <= SMALL_MAX).
 // Every recursion level of the segment runs inside the CTA: the sub-range of
 // position x at depth d follows from (n, p) alone (rank split at
 // lower_count(len, p) while p > 1, then, with LOCAL, halving at len / 2 as
-// rcb_local does), the bounding box of each sub-range comes from a warp-
-// segmented reduction (long sub-ranges, 64-bit atomics into a per-CTA
-// scratch) or a sequential loop (short ones), and the segmented stable sort
-// by (sub-range start, ordered key) is an LSD radix sort in shared memory
-// (warp w ranks items [512 w, 512 w + 512) in order with __match_any_sync).
-// Constant key bytes are skipped.  Gives exactly the order of the level-by-
-// level global path.
+// rcb_local does, src/rcb.c:39-72).  The dense ranks of the segment's
+// elements sit in shared memory for the whole recursion.  Per level:
+//   boxes   - a sequential loop for short sub-ranges, a warp-segmented min /
+//             max plus shared-memory atomics for long ones (table slot
+//             start / SMALL_SHORT: long sub-ranges are disjoint and longer
+//             than SMALL_SHORT, so their slots differ);
+//   axis    - longest edge, uniq[max] - uniq[min] per axis;
+//   order   - stable sort of each sub-range by its axis rank.  When no
+//             sub-range exceeds SMALL_CMP elements, an element's new place
+//             is the number of elements of its sub-range before it in
+//             (rank, position) order; otherwise an LSD radix in shared memory
+//             over the varying bytes of the rank, then of the sub-range start
+//             (warp w ranks positions [512 w, 512 w + 512) in order with
+//             __match_any_sync).
+// Gives exactly the order of the level-by-level global path.
 // ---------------------------------------------------------------------------
 constexpr int SMALL_MAX = 8192;
 constexpr int SMALL_THREADS = 512;
-constexpr int SMALL_ITEMS = 16;  // SMALL_MAX / SMALL_THREADS
+constexpr int SMALL_ITEMS = 16;   // SMALL_MAX / SMALL_THREADS
+constexpr int SMALL_CMP = 256;    // comparison ranking up to this sub-range length
+constexpr int SMALL_SHORT = 32;   // sequential boxes up to this sub-range length
+constexpr int SMALL_NLONG = SMALL_MAX / SMALL_SHORT;  // box table slots
 
 struct SubR {
   int st, len, p, rank;
@@ -413,26 +460,39 @@ __device__ __forceinline__ bool sub_active(const SubR &r) {
   return r.p > 1 || (LOCAL && r.len >= 2);
 }
 
-__device__ __forceinline__ double key_to_double(unsigned long long k) {
-  unsigned long long b = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
-  return __longlong_as_double((long long)b);
+// Items of k_rcb_small: local id in bits 0-15, sub-range start in bits
+// 16-30, bit 31 set while the sub-range is active.
+constexpr u32 ITEM_ACTIVE = 0x80000000u;
+__device__ __forceinline__ u32 item_st(u32 it) { return (it >> 16) & 0x7FFFu; }
+// axis rank of an item; 0 for inactive sub-ranges (their axis slot is unset)
+__device__ __forceinline__ u32 kx_key(const u32 *rk, const unsigned char *sax, u32 it) {
+  return (it & ITEM_ACTIVE) ? rk[sax[item_st(it)] * SMALL_MAX + (it & 0xFFFFu)] : 0u;
+}
+
+// shared memory of k_rcb_small
+constexpr size_t small_smem_bytes() {
+  return (size_t)SMALL_MAX * (3 * 4 /*rk*/ + 4 + 4 /*item, item2*/ + 4 /*kx*/ + 1 /*sax*/) +
+         (size_t)16 * 256 * 2 /*wcnt*/ + (size_t)SMALL_NLONG * 6 * 4 /*box*/;
 }
 
 template <bool LOCAL>
 __global__ void __launch_bounds__(SMALL_THREADS)
-k_rcb_small(int *__restrict__ perm, const double *__restrict__ cent, ll N, int ndim,
+k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
+            const double *__restrict__ uniq, ll N, int ndim,
             const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
             const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
-            unsigned long long *__restrict__ scratch, int *__restrict__ part) {
-  extern __shared__ unsigned long long smem_u64[];
-  u64 *key = smem_u64;                                   // SMALL_MAX
-  u64 *key2 = key + SMALL_MAX;                            // SMALL_MAX
-  unsigned *item = (unsigned *)(key2 + SMALL_MAX);        // (st << 16) | ord
-  unsigned *item2 = item + SMALL_MAX;
-  unsigned short *wcnt = (unsigned short *)(item2 + SMALL_MAX);  // [16][256]
+            int *__restrict__ part) {
+  extern __shared__ u32 smem_u32[];
+  u32 *rk = smem_u32;                  // [3][SMALL_MAX] dense ranks by local id
+  u32 *item = rk + 3 * SMALL_MAX;      // (sub-range start << 16) | local id
+  u32 *item2 = item + SMALL_MAX;
+  u32 *kx = item2 + SMALL_MAX;         // axis rank per position
+  u32 *box = kx + SMALL_MAX;           // [SMALL_NLONG][6] min0..2, max0..2
+  unsigned short *wcnt = (unsigned short *)(box + SMALL_NLONG * 6);  // [16][256]
+  unsigned char *sax = (unsigned char *)(wcnt + 16 * 256);  // axis by sub-range start
   __shared__ unsigned dbase[256];
-  __shared__ unsigned long long s_and, s_or;
-  __shared__ unsigned s_stand, s_stor;
+  __shared__ u32 s_and, s_or, s_stand, s_stor;
+  __shared__ int s_maxlen;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const ll sg = blockIdx.x;
   const ll start = seg_start[sg];
@@ -444,186 +504,237 @@ k_rcb_small(int *__restrict__ perm, const double *__restrict__ cent, ll N, int n
       for (int x = threadIdx.x; x < n; x += blockDim.x) part[perm[start + x]] = r0;
     return;
   }
-  unsigned long long *sc = scratch + start * 6;  // slot = global position of the sub-range start
-  for (int x = threadIdx.x; x < n; x += blockDim.x) item[x] = (unsigned)x;
-  __syncthreads();
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    const int e = perm[start + x];
+    for (int q = 0; q < ndim; q++) rk[q * SMALL_MAX + x] = rank[(ll)q * N + e];
+    item[x] = (u32)x;
+  }
   const unsigned lt_mask = (1u << lane) - 1u;
+  int st_r[SMALL_ITEMS], len_r[SMALL_ITEMS];  // sub-range of each own position
   for (int d = 0; d < 64; d++) {
     // ---- sub-range of each position at depth d
+    if (threadIdx.x == 0) s_maxlen = 0;
+    for (int t = threadIdx.x; t < SMALL_NLONG * 6; t += blockDim.x)
+      box[t] = (t % 6) < 3 ? 0xFFFFFFFFu : 0u;
     bool any = false;
+    int mylen = 0;
+    __syncthreads();
+#pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
       int x = warp * 512 + r * 32 + lane;
-      if (x < n) any |= sub_active<LOCAL>(descend<LOCAL>(x, n, p0, d));
-    }
-    if (!__syncthreads_or(any)) break;
-    // ---- clear bbox slots of active sub-ranges (slot = sub-range start)
-    for (int r = 0; r < SMALL_ITEMS; r++) {
-      int x = warp * 512 + r * 32 + lane;
+      st_r[r] = -1, len_r[r] = 0;
       if (x < n) {
         SubR sr = descend<LOCAL>(x, n, p0, d);
-        if (sr.st == x && sub_active<LOCAL>(sr) && sr.len > 32) {
-          for (int q = 0; q < 3; q++) sc[6 * x + q] = ~0ull, sc[6 * x + 3 + q] = 0ull;
-        }
+        st_r[r] = sr.st;
+        if (sub_active<LOCAL>(sr)) len_r[r] = sr.len, any = true, mylen = max(mylen, sr.len);
       }
     }
-    __syncthreads();
-    // ---- bounding boxes
-    for (int r = 0; r < SMALL_ITEMS; r++) {
-      int x = warp * 512 + r * 32 + lane;
-      bool valid = x < n;
-      SubR sr = valid ? descend<LOCAL>(x, n, p0, d) : SubR{-1, 0, 0, 0};
-      bool act = valid && sub_active<LOCAL>(sr);
-      if (act && sr.len <= 32) {
-        if (sr.st == x) {  // sequential box of a short sub-range
-          u64 mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
-          for (int y = x; y < x + sr.len; y++) {
-            int e = perm[start + (item[y] & 0xFFFF)];
-            for (int q = 0; q < 3; q++) {
-              u64 k = ordered_key(cent[(ll)q * N + e]);
-              mn[q] = k < mn[q] ? k : mn[q];
-              mx[q] = k > mx[q] ? k : mx[q];
-            }
-          }
-          for (int q = 0; q < 3; q++) sc[6 * x + q] = mn[q], sc[6 * x + 3 + q] = mx[q];
-        }
-      }
-      // warp-segmented reduction for long sub-ranges
-      bool lng = act && sr.len > 32;
-      int segkey = lng ? sr.st : -1 - lane;  // unique key for lanes not taking part
-      u64 mn[3], mx[3];
-      int e = lng ? perm[start + (item[x] & 0xFFFF)] : 0;
-      for (int q = 0; q < 3; q++) {
-        u64 k = lng ? ordered_key(cent[(ll)q * N + e]) : 0ull;
-        mn[q] = lng ? k : ~0ull;
-        mx[q] = k;
-      }
+    if (mylen) atomicMax(&s_maxlen, mylen);
+    if (!__syncthreads_or(any)) break;
+    const int maxlen = s_maxlen;
+    // ---- bounding boxes on dense ranks, axis of each sub-range
 #pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        int ok = __shfl_down_sync(0xffffffffu, segkey, off);
-        bool same = (lane + off < 32) && ok == segkey;
-        for (int q = 0; q < 3; q++) {
-          u64 a = __shfl_down_sync(0xffffffffu, mn[q], off);
-          u64 b = __shfl_down_sync(0xffffffffu, mx[q], off);
-          if (same) {
-            mn[q] = a < mn[q] ? a : mn[q];
-            mx[q] = b > mx[q] ? b : mx[q];
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * 512 + r * 32 + lane;
+      const int st = st_r[r], len = len_r[r];
+      if (len > 0 && len <= SMALL_SHORT && st == x) {  // short: sequential
+        u32 mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+        for (int y = x; y < x + len; y++) {
+          const u32 id = item[y] & 0xFFFFu;
+          for (int q = 0; q < ndim; q++) {
+            u32 k = rk[q * SMALL_MAX + id];
+            mn[q] = min(mn[q], k);
+            mx[q] = max(mx[q], k);
           }
         }
-      }
-      // after the down-sweep the first lane of each run holds the run's box
-      int prevkey = __shfl_up_sync(0xffffffffu, segkey, 1);
-      bool head = lane == 0 || prevkey != segkey;
-      if (lng && head) {
-        for (int q = 0; q < 3; q++) {
-          atomicMin(&sc[6 * sr.st + q], mn[q]);
-          atomicMax(&sc[6 * sr.st + 3 + q], mx[q]);
-        }
-      }
-    }
-    __syncthreads();
-    // ---- keys along each sub-range's longest axis
-    if (threadIdx.x == 0) s_and = ~0ull, s_or = 0ull, s_stand = ~0u, s_stor = 0u;
-    __syncthreads();
-    u64 kand = ~0ull, kor = 0ull;
-    unsigned stand = ~0u, stor = 0u;
-    for (int r = 0; r < SMALL_ITEMS; r++) {
-      int x = warp * 512 + r * 32 + lane;
-      if (x >= n) continue;
-      SubR sr = descend<LOCAL>(x, n, p0, d);
-      u64 k = 0ull;
-      if (sub_active<LOCAL>(sr)) {
-        double len[3];
-        for (int q = 0; q < ndim; q++)
-          len[q] = __dsub_rn(key_to_double(sc[6 * sr.st + 3 + q]), key_to_double(sc[6 * sr.st + q]));
+        double best = 0.0;
         int ax = 0;
-        for (int q = 1; q < ndim; q++)
-          if (len[q] > len[ax]) ax = q;
-        int e = perm[start + (item[x] & 0xFFFF)];
-        k = ordered_key(cent[(ll)ax * N + e]);
+        for (int q = 0; q < ndim; q++) {
+          double l = __dsub_rn(uniq[(ll)q * N + mx[q]], uniq[(ll)q * N + mn[q]]);
+          if (q == 0 || l > best) best = l, ax = q;
+        }
+        sax[x] = (unsigned char)ax;
       }
-      key[x] = k;
-      item[x] = ((unsigned)sr.st << 16) | (item[x] & 0xFFFF);
-      kand &= k, kor |= k;
-      stand &= (unsigned)sr.st, stor |= (unsigned)sr.st;
+      if (maxlen > SMALL_SHORT) {  // warp-uniform
+        const bool lng = len > SMALL_SHORT;
+        const int segkey = lng ? st : -1 - lane;
+        u32 mn[3], mx[3];
+        const u32 id = lng ? (item[x] & 0xFFFFu) : 0u;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          u32 k = (lng && q < ndim) ? rk[q * SMALL_MAX + id] : 0u;
+          mn[q] = lng ? k : 0xFFFFFFFFu;
+          mx[q] = k;
+        }
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          int ok = __shfl_down_sync(0xffffffffu, segkey, off);
+          bool same = (lane + off < 32) && ok == segkey;
+#pragma unroll
+          for (int q = 0; q < 3; q++) {
+            u32 a2 = __shfl_down_sync(0xffffffffu, mn[q], off);
+            u32 b2 = __shfl_down_sync(0xffffffffu, mx[q], off);
+            if (same) mn[q] = min(mn[q], a2), mx[q] = max(mx[q], b2);
+          }
+        }
+        int prevkey = __shfl_up_sync(0xffffffffu, segkey, 1);
+        bool head = lane == 0 || prevkey != segkey;
+        if (lng && head) {
+          const int o = st / SMALL_SHORT;
+          for (int q = 0; q < ndim; q++) {
+            atomicMin(&box[6 * o + q], mn[q]);
+            atomicMax(&box[6 * o + 3 + q], mx[q]);
+          }
+        }
+      }
     }
-    atomicAnd(&s_and, kand);
-    atomicOr(&s_or, kor);
-    atomicAnd(&s_stand, stand);
-    atomicOr(&s_stor, stor);
     __syncthreads();
-    u64 kdiff = s_and ^ s_or;
-    unsigned sdiff = s_stand ^ s_stor;
-    // ---- stable LSD passes: key bytes, then sub-range start bytes
-    for (int b = 0; b < 10; b++) {
-      bool is_st = b >= 8;
-      int shift = is_st ? 8 * (b - 8) : 8 * b;
-      if (is_st ? ((sdiff >> shift) & 255u) == 0 : ((kdiff >> shift) & 255ull) == 0) continue;
-      for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) wcnt[i] = 0;
-      __syncthreads();
-      unsigned rk[SMALL_ITEMS], dg[SMALL_ITEMS];
+    if (maxlen > SMALL_SHORT) {
 #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
-        int x = warp * 512 + r * 32 + lane;
-        unsigned dgt = 256;
-        if (x < n)
-          dgt = is_st ? ((item[x] >> 16) >> shift) & 255u : (unsigned)(key[x] >> shift) & 255u;
-        unsigned peers = __match_any_sync(0xffffffffu, dgt);
-        unsigned before = 0;
-        if (dgt < 256) before = wcnt[warp * 256 + dgt];
-        __syncwarp();
-        if (dgt < 256) {
-          rk[r] = before + __popc(peers & lt_mask);
-          if (lane == __ffs(peers) - 1) wcnt[warp * 256 + dgt] = (unsigned short)(before + __popc(peers));
-        }
-        dg[r] = dgt;
-        __syncwarp();
-      }
-      __syncthreads();
-      if (threadIdx.x < 256) {
-        unsigned run = 0;
-        for (int w = 0; w < 16; w++) {
-          unsigned t = wcnt[w * 256 + threadIdx.x];
-          wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
-          run += t;
-        }
-        dbase[threadIdx.x] = run;  // total of this digit (scanned below)
-      }
-      __syncthreads();
-      if (threadIdx.x < 32) {  // exclusive scan of the 256 digit totals
-        unsigned v[8], s2 = 0;
-        for (int j = 0; j < 8; j++) v[j] = dbase[threadIdx.x * 8 + j], s2 += v[j];
-        unsigned incl = s2;
-        for (int o = 1; o < 32; o <<= 1) {
-          unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (threadIdx.x >= o) incl += y;
-        }
-        unsigned run = incl - s2;
-        for (int j = 0; j < 8; j++) dbase[threadIdx.x * 8 + j] = run, run += v[j];
-      }
-      __syncthreads();
-#pragma unroll
-      for (int r = 0; r < SMALL_ITEMS; r++) {
-        int x = warp * 512 + r * 32 + lane;
-        if (x < n) {
-          unsigned pos = dbase[dg[r]] + wcnt[warp * 256 + dg[r]] + rk[r];
-          key2[pos] = key[x];
-          item2[pos] = item[x];
+        const int x = warp * 512 + r * 32 + lane;
+        if (len_r[r] > SMALL_SHORT && st_r[r] == x) {
+          const int o = x / SMALL_SHORT;
+          double best = 0.0;
+          int ax = 0;
+          for (int q = 0; q < ndim; q++) {
+            double l = __dsub_rn(uniq[(ll)q * N + box[6 * o + 3 + q]],
+                                 uniq[(ll)q * N + box[6 * o + q]]);
+            if (q == 0 || l > best) best = l, ax = q;
+          }
+          sax[x] = (unsigned char)ax;
         }
       }
-      __syncthreads();
-      for (int x = threadIdx.x; x < n; x += blockDim.x) key[x] = key2[x], item[x] = item2[x];
       __syncthreads();
     }
-    for (int x = threadIdx.x; x < n; x += blockDim.x) item[x] &= 0xFFFF;
+    // ---- keys: rank along the sub-range's axis
+    u32 kand = 0xFFFFFFFFu, kor = 0u, stand = 0xFFFFFFFFu, stor = 0u;
+#pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * 512 + r * 32 + lane;
+      if (x >= n) continue;
+      const u32 st = (u32)st_r[r];
+      const u32 id = item[x] & 0xFFFFu;
+      const u32 k = len_r[r] ? rk[sax[st] * SMALL_MAX + id] : 0u;
+      kx[x] = k;
+      item[x] = (st << 16) | id | (len_r[r] ? ITEM_ACTIVE : 0u);
+      kand &= k, kor |= k, stand &= st, stor |= st;
+    }
     __syncthreads();
+    if (maxlen <= SMALL_CMP) {
+      // ---- comparison ranking inside each sub-range
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * 512 + r * 32 + lane;
+        if (x >= n) continue;
+        const int len = len_r[r], st = st_r[r];
+        if (!len) {
+          item2[x] = item[x];
+          continue;
+        }
+        const u32 k = kx[x];
+        int c = 0;
+        for (int y = st; y < st + len; y++) {
+          const u32 k2 = kx[y];
+          c += (k2 < k) || (k2 == k && y < x);
+        }
+        item2[st + c] = item[x];
+      }
+      __syncthreads();
+      u32 *t = item;
+      item = item2;
+      item2 = t;
+    } else {
+      // ---- stable LSD passes over the varying bytes: rank, then start
+      if (threadIdx.x == 0) s_and = 0xFFFFFFFFu, s_or = 0u, s_stand = 0xFFFFFFFFu, s_stor = 0u;
+      __syncthreads();
+      atomicAnd(&s_and, kand);
+      atomicOr(&s_or, kor);
+      atomicAnd(&s_stand, stand);
+      atomicOr(&s_stor, stor);
+      __syncthreads();
+      const u32 kdiff = s_and ^ s_or, sdiff = s_stand ^ s_stor;
+      for (int b = 0; b < 6; b++) {
+        const bool is_st = b >= 4;
+        const int shift = is_st ? 8 * (b - 4) : 8 * b;
+        if ((((is_st ? sdiff : kdiff) >> shift) & 255u) == 0) continue;
+        for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) wcnt[i] = 0;
+        __syncthreads();
+        unsigned rkk[SMALL_ITEMS], dg[SMALL_ITEMS];
+        u32 itv[SMALL_ITEMS];
+#pragma unroll
+        for (int r = 0; r < SMALL_ITEMS; r++) {
+          const int x = warp * 512 + r * 32 + lane;
+          unsigned dgt = 256;
+          itv[r] = 0;
+          if (x < n) {
+            const u32 it = item[x];
+            itv[r] = it;
+            // inactive positions carry key 0 (their sub-range keeps its order)
+            const u32 k = is_st ? item_st(it) : kx_key(rk, sax, it);
+            dgt = (k >> shift) & 255u;
+          }
+          unsigned peers = __match_any_sync(0xffffffffu, dgt);
+          unsigned before = 0;
+          if (dgt < 256) before = wcnt[warp * 256 + dgt];
+          __syncwarp();
+          if (dgt < 256) {
+            rkk[r] = before + __popc(peers & lt_mask);
+            if (lane == __ffs(peers) - 1)
+              wcnt[warp * 256 + dgt] = (unsigned short)(before + __popc(peers));
+          }
+          dg[r] = dgt;
+          __syncwarp();
+        }
+        __syncthreads();
+        if (threadIdx.x < 256) {
+          unsigned run = 0;
+          for (int w = 0; w < 16; w++) {
+            unsigned t = wcnt[w * 256 + threadIdx.x];
+            wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
+            run += t;
+          }
+          dbase[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // exclusive scan of the 256 digit totals
+          unsigned v[8], s2 = 0;
+          for (int j = 0; j < 8; j++) v[j] = dbase[threadIdx.x * 8 + j], s2 += v[j];
+          unsigned incl = s2;
+          for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (threadIdx.x >= o) incl += y;
+          }
+          unsigned run = incl - s2;
+          for (int j = 0; j < 8; j++) dbase[threadIdx.x * 8 + j] = run, run += v[j];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < SMALL_ITEMS; r++) {
+          if (dg[r] < 256) item2[dbase[dg[r]] + wcnt[warp * 256 + dg[r]] + rkk[r]] = itv[r];
+        }
+        __syncthreads();
+        u32 *t = item;
+        item = item2;
+        item2 = t;
+      }
+    }
   }
-  // ---- write the order (and ranks) back
-  int *tmp = (int *)key2;
-  for (int x = threadIdx.x; x < n; x += blockDim.x) tmp[x] = perm[start + (item[x] & 0xFFFF)];
+  // ---- write the order (and ranks) back: read every old entry, then write
+  int ev[SMALL_ITEMS];
+#pragma unroll
+  for (int r = 0; r < SMALL_ITEMS; r++) {
+    const int x = warp * 512 + r * 32 + lane;
+    ev[r] = x < n ? perm[start + (item[x] & 0xFFFFu)] : 0;
+  }
   __syncthreads();
-  for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    perm[start + x] = tmp[x];
-    if (part) part[tmp[x]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+#pragma unroll
+  for (int r = 0; r < SMALL_ITEMS; r++) {
+    const int x = warp * 512 + r * 32 + lane;
+    if (x < n) {
+      perm[start + x] = ev[r];
+      if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+    }
   }
 }
 
@@ -696,7 +807,27 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
   ws.vals.ensure((size_t)N);
   DBuf<int> nact_d(1);
   DBuf<unsigned long long> maxn_d(1);
-  const size_t small_smem = (size_t)SMALL_MAX * (8 + 8 + 4 + 4) + 16 * 256 * 2;
+  const size_t small_smem = small_smem_bytes();
+  if (kind == BISECT_RCB && ws.rank_of != cent) {
+    // dense ranks of the centroid coordinates, once per set of centroids
+    ws.rank.ensure((size_t)3 * N);
+    ws.uniq.ensure((size_t)3 * N);
+    DBuf<int> flag((size_t)N);
+    DBuf<ll> excl((size_t)N);
+    for (int a = 0; a < ndim; a++) {
+      k_axis_keys<<<grid_for(N, 256), 256, 0, st>>>(cent, N, a, ws.keys.p, ws.vals.p);
+      CK_LAUNCH();
+      seg_sort_pairs(ws.keys, ws.vals, N, nullptr, 1, ws.sort);
+      k_rank_flags<<<grid_for(N, 256), 256, 0, st>>>(ws.keys.p, N, flag.p);
+      CK_LAUNCH();
+      exclusive_scan_int_to_ll(flag.p, excl.p, N);
+      k_rank_write<<<grid_for(N, 256), 256, 0, st>>>(ws.keys.p, ws.vals.p, flag.p, excl.p, N,
+                                                      ws.rank.p + (ll)a * N,
+                                                      ws.uniq.p + (ll)a * N);
+      CK_LAUNCH();
+    }
+    ws.rank_of = cent;
+  }
   for (int level = 0; level < 200; level++) {
     ll nseg = t.count;
     // active segments, their largest size, and children counts
@@ -715,17 +846,18 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
     sync();
     if (kind == BISECT_RCB && nact > 0 && maxn <= (unsigned long long)SMALL_MAX) {
       // every remaining level of every segment in one launch
-      DBuf<unsigned long long> scratch((size_t)N * 6);
       if (do_local) {
         CK(cudaFuncSetAttribute(k_rcb_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)small_smem));
         k_rcb_small<true><<<(unsigned)nseg, SMALL_THREADS, small_smem, st>>>(
-            perm.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p, scratch.p, part_of_elem);
+            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
       } else {
         CK(cudaFuncSetAttribute(k_rcb_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)small_smem));
         k_rcb_small<false><<<(unsigned)nseg, SMALL_THREADS, small_smem, st>>>(
-            perm.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p, scratch.p, part_of_elem);
+            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
       }
       CK_LAUNCH();
       return;
@@ -740,7 +872,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
                                                       do_local, ws.axis.p);
       CK_LAUNCH();
       k_keys<BISECT_RCB><<<grid_for(N, 256), 256, 0, st>>>(
-          perm.p, cent, N, ws.seg_of_pos.p, ws.axis.p, nullptr, nullptr, ws.keys.p,
+          perm.p, cent, ws.rank.p, N, ws.seg_of_pos.p, ws.axis.p, nullptr, nullptr, ws.keys.p,
           ws.vals.p, ws.seg_of_elem.p);
       CK_LAUNCH();
     } else {
@@ -762,7 +894,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
           avg.p, isums.p, ws.ev.p, ws.axis.p);
       CK_LAUNCH();
       k_keys<BISECT_RIB><<<grid_for(N, 256), 256, 0, st>>>(
-          perm.p, cent, N, ws.seg_of_pos.p, ws.axis.p, avg.p, ws.ev.p, ws.keys.p,
+          perm.p, cent, nullptr, N, ws.seg_of_pos.p, ws.axis.p, avg.p, ws.ev.p, ws.keys.p,
           ws.vals.p, ws.seg_of_elem.p);
       CK_LAUNCH();
     }

@@ -21,6 +21,11 @@ struct BisectWs {
   DBuf<ll> tile_off, child_off;
   DBuf<int> child_cnt;
   SegTable t2;
+  // RCB: dense rank of every centroid coordinate per axis (3 x N) and the
+  // distinct values by rank (3 x N), built once for the centroids `rank_of`
+  DBuf<u32> rank;
+  DBuf<double> uniq;
+  const double *rank_of = nullptr;
 };
 
 // Recursive bisection of every segment of `t` (segments tile [0, N) of the
