@@ -152,6 +152,13 @@ __global__ void k_ell_count(const int *__restrict__ perm, const int *__restrict_
   rowlen[i] = cnt;
 }
 
+__global__ void k_max_int(const int *__restrict__ a, ll n, int *__restrict__ mx) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  int v = i < n ? a[i] : 0;
+  for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(mx, v);
+}
+
 __global__ void k_slice_w(const int *__restrict__ rowlen, ll N, ll nslice,
                           ll *__restrict__ slots, int *__restrict__ width) {
   ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
@@ -775,6 +782,158 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
 }
 
+// ---------------------------------------------------------------------------
+// SpMV with the index stream staged by the Tensor Memory Accelerator.
+// Same arithmetic and reduction order as k_spmv (bitwise the same w and tile
+// partials), but the ELL words of SP_SS consecutive slices are copied into
+// shared memory by one cp.async.bulk per stage (SP_NST stages in flight,
+// completion counted on an mbarrier), so the warps only wait on the gathers
+// of p, never on the DRAM latency of the index stream.  Warp w handles slice
+// w of every stage.  A wait gives up after about two seconds of clock and
+// sets err[0]; every thread still meets every __syncthreads.
+// ---------------------------------------------------------------------------
+constexpr int SP_NST = 3;  // stages in flight per block
+
+__device__ __forceinline__ u32 smem_u32addr(const void *p) {
+  return (u32)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(u32 bar, u32 count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(u32 bar, u32 bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(u32 bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(u32 bar, u32 parity) {
+  u32 ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false after ~2 s of SM clock
+__device__ __forceinline__ bool mbar_wait(u32 bar, u32 parity) {
+  if (mbar_test(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (clock64() - t0 > 4000000000ll) return false;
+    __nanosleep(20);
+  }
+  return true;
+}
+__device__ __forceinline__ void bulk_g2s(u32 dst, const void *src, u32 bytes, u32 bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(512)
+k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
+           const int *__restrict__ tgrp, GState *__restrict__ gs,
+           const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+           const int *__restrict__ slice_w, const float *__restrict__ p, float *__restrict__ w,
+           double *__restrict__ part, FinArgs fa, int fuse, int force, int stage_bytes,
+           int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char sp_smem[];
+  __shared__ double sh[32];
+  __shared__ double cs[LZ_TILE / 32 + 1];
+  __shared__ ll soff[LZ_TILE / 32 + 2];
+  __shared__ __align__(8) unsigned long long bars[SP_NST];
+  __shared__ int s_bad;
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
+  if (!gs[g].run && !force) return;
+  const float c = (float)gs[g].c;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const ll b = tbeg[t], e = tend[t];
+  const ll c0 = b >> 5;
+  const int nc = (int)(((e - 1) >> 5) - c0 + 1);
+  const int nst = (nc + nw - 1) / nw;  // stages of nw slices
+  for (int q = threadIdx.x; q <= nc; q += blockDim.x) soff[q] = slice_off[c0 + q];
+  if (threadIdx.x == 0) {
+    s_bad = 0;
+    for (int k = 0; k < SP_NST; k++) mbar_init(smem_u32addr(&bars[k]), 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](int j) {  // thread 0: stage j into buffer j % SP_NST
+    const int q0 = j * nw, q1 = min(q0 + nw, nc);
+    const u32 bytes = (u32)((soff[q1] - soff[q0]) * 4);
+    const u32 bar = smem_u32addr(&bars[j % SP_NST]);
+    if (bytes > (u32)stage_bytes) {  // never copy past the stage buffer
+      s_bad = 1;
+      mbar_arrive(bar);
+    } else if (bytes == 0) {
+      mbar_arrive(bar);
+    } else {
+      mbar_expect_tx(bar, bytes);
+      bulk_g2s(smem_u32addr(sp_smem + (size_t)(j % SP_NST) * stage_bytes), ell + soff[q0],
+               bytes, bar);
+    }
+  };
+  if (threadIdx.x == 0)
+    for (int j = 0; j < SP_NST && j < nst; j++) issue(j);
+  for (int j = 0; j < nst; j++) {
+    const int buf = j % SP_NST;
+    if (!mbar_wait(smem_u32addr(&bars[buf]), (u32)((j / SP_NST) & 1))) s_bad = 1;
+    const int q = j * nw + warp;
+    if (q < nc && !s_bad) {
+      const ll sl = c0 + q;
+      const ll i = sl * 32 + lane;
+      const bool valid = i >= b && i < e;
+      const int wd = valid ? slice_w[sl] : 0;
+      const float pi = valid ? p[i] : 0.f;
+      const unsigned *ep = reinterpret_cast<const unsigned *>(
+                               sp_smem + (size_t)buf * stage_bytes) +
+                           (soff[q] - soff[j * nw]) + lane;
+      float sum = 0.f;
+      int k = 0;
+#pragma unroll 1
+      for (; k + 8 <= wd; k += 8) {
+        unsigned x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = ep[(k + u) * 32];
+        float pj[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) pj[u] = p[x[u] & 0x0FFFFFFFu];
+#pragma unroll
+        for (int u = 0; u < 8; u++) sum = fmaf(small_u2f(x[u] >> 28), pi - pj[u], sum);
+      }
+      for (; k < wd; k++) {
+        unsigned x = ep[k * 32];
+        sum = fmaf(small_u2f(x >> 28), pi - p[x & 0x0FFFFFFFu], sum);
+      }
+      Term<float> tv;
+      if (valid) {
+        w[i] = sum;
+        tv.set_prod(sum, pi - c);
+      }
+      double v = tv.chunk();
+      if (lane == 0) cs[q] = v;
+    } else if (q < nc && lane == 0) {
+      cs[q] = 0.0;
+    }
+    __syncthreads();  // buffer j % SP_NST is free again
+    if (threadIdx.x == 0 && j + SP_NST < nst) issue(j + SP_NST);
+  }
+  if (threadIdx.x == 0) {
+    if (s_bad) atomicExch(err, 1);
+    part[t] = tile_total(cs, nc);
+  }
+  if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
+}
+
 // Ritz vector f_i = sum_j coef_j V_j[i] (j < iters, src/fiedler.c:520-535)
 // and the tile partial of sum f, R rows per lane (16-byte loads of each
 // basis row).  FP32: compensated dot (Ogita, Rump and Oishi's Dot2) with each
@@ -1106,6 +1265,7 @@ struct Level {
   DBuf<int> slice_w;
   ll nnz = 0;    // restricted nonzeros of the active rows
   ll rows = 0;   // active rows
+  int max_w = 0; // widest slice
 };
 
 template <typename VT>
@@ -1125,6 +1285,8 @@ struct Lanczos {
   std::vector<cudaEvent_t> ev;  // SpMV start/stop events (timing mode)
   std::vector<cudaEvent_t> evk; // p / r per step, then init, eig, ritz (timing mode)
   int bd = 256;                  // threads per tile block (autotuned per level)
+  int sp_kind = 0;               // SpMV variant: 0 k_spmv, 1 k_spmv_tma (autotuned)
+  DBuf<int> err;                 // [0]: a staged-SpMV wait gave up
   int pr_bd = 256;               // threads per block of k_pr
   int ritz_bd = 256;             // threads per block of k_ritz
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
@@ -1171,6 +1333,8 @@ struct Lanczos {
     diagT.ensure((size_t)A * MI), upperT.ensure((size_t)A * MI);
     vnorm.ensure((size_t)A * (MI + 1)), coef.ensure((size_t)A * MI);
     any.ensure(2);
+    err.ensure(1);
+    CK(cudaMemsetAsync(err.p, 0, sizeof(int), ctx().stream));
     cnt.ensure(A);
     CK(cudaMemsetAsync(cnt.p, 0, (size_t)A * sizeof(int), ctx().stream));
 
@@ -1243,10 +1407,7 @@ struct Lanczos {
       CK_LAUNCH();
       mark(4 * it + 1);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
-      k_spmv<VT><<<T, bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
-                                   lv.slice_w.p, p.p, w.p, part.p, fargs(it, tol, mpass), 1,
-                                   0);
-      CK_LAUNCH();
+      spmv(lv, sp_kind, bd, fargs(it, tol, mpass), 1, 0);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       mark(4 * it + 2);
@@ -1269,46 +1430,77 @@ struct Lanczos {
     fin<FIN_PASS_END, GATE_ACTIVE>(0, tol, mpass);
   }
 
+  // shared memory of one k_spmv_tma stage (nw slices of the widest width)
+  static size_t sp_stage_bytes(const Level &lv, int threads) {
+    return (size_t)(threads / 32) * (size_t)std::max(lv.max_w, 1) * 128;
+  }
+  bool sp_tma_ok(const Level &lv, int threads) const {
+    return sizeof(VT) == 4 && SP_NST * sp_stage_bytes(lv, threads) <= 200 * 1024;
+  }
+  void spmv(const Level &lv, int kind, int threads, const FinArgs &fa, int fuse, int force) {
+    cudaStream_t st = ctx().stream;
+    if (kind == 1 && sizeof(VT) == 4) {
+      const size_t sb = sp_stage_bytes(lv, threads);
+      k_spmv_tma<<<T, threads, SP_NST * sb, st>>>(
+          tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p,
+          reinterpret_cast<const float *>(p.p), reinterpret_cast<float *>(w.p), part.p, fa, fuse,
+          force, (int)sb, err.p);
+    } else {
+      k_spmv<VT><<<T, threads, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
+                                        lv.slice_w.p, p.p, w.p, part.p, fa, fuse, force);
+    }
+    CK_LAUNCH();
+  }
+
   // Autotuner: threads per tile block for this level.  Candidates are timed
   // on the level's own matrix (three forced SpMV launches each, CUDA
   // events); the tile reductions are canonical, so the choice never changes
   // a result.  Decisions are cached per (tiles, groups, rows) for the thread.
   void autotune(const Level &lv) {
-    static thread_local std::vector<std::pair<std::array<ll, 3>, int>> cache;
-    std::array<ll, 3> key = {(ll)T, (ll)A, N};
+    // PARRSB_GPU_SPMV: 0 = k_spmv only, 1 = k_spmv_tma only, unset = time both
+    const char *force_env = getenv("PARRSB_GPU_SPMV");
+    const int force_kind = force_env ? atoi(force_env) : -1;
+    static thread_local std::vector<std::pair<std::array<ll, 5>, int>> cache;
+    std::array<ll, 5> key = {(ll)T, (ll)A, N, (ll)lv.max_w, (ll)force_kind};
     for (auto &kv : cache)
       if (kv.first == key) {
-        bd = kv.second;
+        sp_kind = kv.second >> 16;
+        bd = kv.second & 0xFFFF;
         return;
       }
     cudaStream_t st = ctx().stream;
-    const int cand[3] = {128, 256, 512};
+    static bool attr_set = false;
+    if (!attr_set) {
+      CK(cudaFuncSetAttribute(k_spmv_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              200 * 1024));
+      attr_set = true;
+    }
+    std::vector<std::pair<int, int>> cand;
+    for (int th : {128, 256, 512}) {
+      if (force_kind < 0 || force_kind == 0) cand.push_back({0, th});
+      if ((force_kind < 0 || force_kind == 1) && sp_tma_ok(lv, th)) cand.push_back({1, th});
+    }
+    if (cand.empty()) cand.push_back({0, 256});
     float best = 1e30f;
-    int pick = 256;
+    std::pair<int, int> pick = cand[0];
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    for (int ci = 0; ci < 3; ci++) {
-      int b = cand[ci];
-      k_spmv<VT><<<T, b, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
-                                  lv.slice_w.p, p.p, w.p, part.p, fargs(0, 0.0, 0), 0, 1);
-      CK_LAUNCH();
+    for (auto &c : cand) {
+      spmv(lv, c.first, c.second, fargs(0, 0.0, 0), 0, 1);
       CK(cudaEventRecord(e0, st));
-      for (int rep = 0; rep < 3; rep++) {
-        k_spmv<VT><<<T, b, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
-                                    lv.slice_w.p, p.p, w.p, part.p, fargs(0, 0.0, 0), 0, 1);
-        CK_LAUNCH();
-      }
+      for (int rep = 0; rep < 3; rep++) spmv(lv, c.first, c.second, fargs(0, 0.0, 0), 0, 1);
       CK(cudaEventRecord(e1, st));
       CK(cudaEventSynchronize(e1));
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best * 0.97f) best = ms, pick = b;
+      if (ms < best * 0.97f) best = ms, pick = c;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    bd = pick;
-    cache.push_back({key, pick});
+    sp_kind = pick.first;
+    bd = pick.second;
+    cache.push_back({key, (pick.first << 16) | pick.second});
   }
 
   // Runs all passes; f holds the normalised Fiedler vectors afterwards.
@@ -1383,6 +1575,12 @@ struct Lanczos {
     ctx().stats.spmv_launches += launches;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    {
+      int h_err = 0;
+      d2h(&h_err, err.p, 1);
+      sync();
+      if (h_err) throw CudaError{cudaErrorLaunchTimeout, __FILE__, __LINE__};  // a stage wait gave up
+    }
     // normalise (src/fiedler.c:606-613), then fix the sign canonically:
     // sum_i s_i f_i >= 0 with s = +1 on the first half of the group's order
     tile<TM_SQ_F, GATE_ALL>();
@@ -1625,6 +1823,7 @@ void build_level(const Graph &g, const int *perm, const int *inv, const int *grp
   k_slice_w<<<grid_for(nslice, 256), 256, 0, st>>>(rowlen.p, N, nslice, slots.p, lv.slice_w.p);
   CK_LAUNCH();
   ll total = exclusive_scan_ll(slots.p, lv.slice_off.p, nslice);
+  h2d(lv.slice_off.p + nslice, &total, 1);  // end of the last slice
   lv.ell.ensure((size_t)total + 32);
   k_ell_fill<<<grid_for(N, 256), 256, 0, st>>>(perm, inv, grp, g.rowptr.p, g.col.p, g.w.p, N,
                                                lv.slice_off.p, lv.slice_w.p, lv.ell.p);
@@ -1636,6 +1835,12 @@ void build_level(const Graph &g, const int *perm, const int *inv, const int *grp
   (void)hr;
   ll nnz = exclusive_scan_int_to_ll(rowlen.p, rl64.p, N);
   lv.nnz = nnz;
+  DBuf<int> mw(1);
+  CK(cudaMemsetAsync(mw.p, 0, sizeof(int), st));
+  k_max_int<<<grid_for(nslice, 256), 256, 0, st>>>(lv.slice_w.p, nslice, mw.p);
+  CK_LAUNCH();
+  d2h(&lv.max_w, mw.p, 1);
+  sync();
 }
 
 template <typename VT>

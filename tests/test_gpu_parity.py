@@ -220,3 +220,16 @@ def test_rsb_plain_equals_batched(monkeypatch):
     monkeypatch.setenv("PARRSB_GPU_BATCHED", "0")
     b = P.part_mesh(vtx, xyz, 6, partitioner=0)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("shape,nparts", [((24, 20, 16), 8), ((64, 64, 32), 4)])
+def test_rsb_staged_spmv_bitwise(monkeypatch, shape, nparts):
+    """The TMA-staged SpMV (index stream copied to shared memory by
+    cp.async.bulk) gives bitwise the partition of the plain SpMV."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", "1")
+    vtx, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=12)
+    monkeypatch.setenv("PARRSB_GPU_SPMV", "0")
+    a = P.part_mesh(vtx, xyz, nparts, partitioner=0)
+    monkeypatch.setenv("PARRSB_GPU_SPMV", "1")
+    b = P.part_mesh(vtx, xyz, nparts, partitioner=0)
+    np.testing.assert_array_equal(a, b)
