@@ -32,11 +32,13 @@ namespace prsb {
 namespace {
 
 constexpr int LZ_THREADS = 256;
-constexpr ll LZ_TILE = 2048;  // largest tile (rows); smaller groups use 512
+constexpr ll LZ_TILE = 8192;  // largest tile (rows)
 
 // Rows per tile of a group of n rows: big groups keep few partials per
 // reduction, smaller ones get enough blocks to fill the GPU.
-inline ll tile_rows(ll n) { return n >= (1ll << 20) ? LZ_TILE : 512; }
+inline ll tile_rows(ll n) {
+  return n >= (1ll << 22) ? LZ_TILE : n >= (1ll << 16) ? 2048 : 512;
+}
 constexpr int MAX_MITER = 120;
 
 // ----------------------------------------------------------------------------
@@ -269,8 +271,16 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
   if (OP != FIN_PASS_END) {
     for (int v = 0; v < nv; v++) {
       double acc = 0.0;
-      for (int q = threadIdx.x; q < s.ntiles; q += blockDim.x)
-        acc = __dadd_rn(acc, __ldcg(&part[(ll)nv * (s.tile0 + q) + v]));
+      const int bd = blockDim.x;
+      int q = threadIdx.x;
+      for (; q + 7 * bd < s.ntiles; q += 8 * bd) {  // eight loads in flight, same order
+        double x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = __ldcg(&part[(ll)nv * (s.tile0 + q + u * bd) + v]);
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc = __dadd_rn(acc, x[u]);
+      }
+      for (; q < s.ntiles; q += bd) acc = __dadd_rn(acc, __ldcg(&part[(ll)nv * (s.tile0 + q) + v]));
       tot[v] = block_sum(acc, sh);
       __syncthreads();
     }
@@ -444,11 +454,13 @@ __device__ __forceinline__ double Term<float>::chunk() const { return chunk_sum_
 template <>
 __device__ __forceinline__ double Term<double>::chunk() const { return warp_tree_sum(s + c); }
 
-// Sum of chunk values cs[0..nc) in order (thread 0).
+// Tile partial from its chunk values cs[0..nc), run by warp 0: lane l sums
+// cs[l], cs[l + 32], ... in order, then the fixed shuffle tree; the result
+// (lane 0) depends only on the chunk values, never on the CTA size.
 __device__ __forceinline__ double tile_total(const double *cs, int nc) {
   double t = 0.0;
-  for (int q = 0; q < nc; q++) t = __dadd_rn(t, cs[q]);
-  return t;
+  for (int q = threadIdx.x & 31; q < nc; q += 32) t = __dadd_rn(t, cs[q]);
+  return warp_tree_sum(t);
 }
 
 template <typename VT, int MODE, int GATE, int FUSE>
@@ -530,12 +542,13 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   }
   if (has_sum) {
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
       if (MODE == TM_RESID1) {
-        part[2 * t] = tile_total(cs[0], nc);
-        part[2 * t + 1] = tile_total(cs[1], nc);
+        double v0 = tile_total(cs[0], nc), v1 = tile_total(cs[1], nc);
+        if (threadIdx.x == 0) part[2 * t] = v0, part[2 * t + 1] = v1;
       } else {
-        part[t] = tile_total(cs[0], nc);
+        double v0 = tile_total(cs[0], nc);
+        if (threadIdx.x == 0) part[t] = v0;
       }
     }
     if (FUSE >= 0) fused_fin<FUSE>(gs, g, part, fa, sh);
@@ -611,12 +624,14 @@ template <>
 __device__ __forceinline__ double LaneSum<double>::chunk() const { return warp_tree_sum(s); }
 
 // The two vector updates of a Lanczos step (src/fiedler.c:233-262, CG form),
-// R consecutive rows per lane and two chunks of 32 R rows per warp in flight
+// R consecutive rows per lane and PR_U chunks of 32 R rows per warp in flight
 // (16-byte loads).  r is row `it` of the Krylov basis V.
 //   TM_P: p = r (it 0) or beta (p - c) + r; tile partial of sum p
 //   TM_R: V[it+1] = V[it] - alpha w; tile partial of sum V[it+1]^2
 // The chunk decomposition (32 R rows, aligned to multiples of 32 R) does not
 // depend on the CTA size.  The last tile block of a group finalises it.
+constexpr int PR_U = 4;  // chunks per warp in flight in k_pr
+
 template <typename VT, int MODE>
 __global__ void __launch_bounds__(512)
 k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
@@ -639,21 +654,20 @@ k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__rest
   const ll b = tbeg[t], e = tend[t];
   const ll c0 = b / CH;
   const int nc = (int)((e - 1) / CH - c0 + 1);
-  for (int q0 = 2 * warp; q0 < nc; q0 += 2 * nw) {
-    const bool two = q0 + 1 < nc;  // warp-uniform
-    ll i0[2];
-    VT x[2][R], y[2][R];
+  for (int q0 = PR_U * warp; q0 < nc; q0 += PR_U * nw) {
+    ll i0[PR_U];
+    VT x[PR_U][R], y[PR_U][R];
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
+    for (int u = 0; u < PR_U; u++) {
       i0[u] = (c0 + q0 + u) * CH + (ll)lane * R;
-      if (u == 0 || two) {
+      if (q0 + u < nc) {  // warp-uniform
         load_rows(rv, i0[u], b, e, x[u]);
         if (MODE == TM_R || it > 0) load_rows(MODE == TM_P ? (const VT *)p : w, i0[u], b, e, y[u]);
       }
     }
 #pragma unroll
-    for (int u = 0; u < 2; u++) {
-      if (u == 1 && !two) break;
+    for (int u = 0; u < PR_U; u++) {
+      if (q0 + u >= nc) break;
       LaneSum<VT> acc;
       VT o[R];
 #pragma unroll
@@ -674,7 +688,10 @@ k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__rest
     }
   }
   __syncthreads();
-  if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
+  if (threadIdx.x < 32) {
+    double v0 = tile_total(cs, nc);
+    if (threadIdx.x == 0) part[t] = v0;
+  }
   fused_fin<OP>(gs, g, part, fa, sh);
 }
 
@@ -778,7 +795,10 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     if (lane == 0) cs[q] = v;
   }
   __syncthreads();
-  if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
+  if (threadIdx.x < 32) {
+    double v0 = tile_total(cs, nc);
+    if (threadIdx.x == 0) part[t] = v0;
+  }
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
 }
 
@@ -927,9 +947,12 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     __syncthreads();  // buffer j % SP_NST is free again
     if (threadIdx.x == 0 && j + SP_NST < nst) issue(j + SP_NST);
   }
-  if (threadIdx.x == 0) {
-    if (s_bad) atomicExch(err, 1);
-    part[t] = tile_total(cs, nc);
+  if (threadIdx.x < 32) {
+    double v0 = tile_total(cs, nc);
+    if (threadIdx.x == 0) {
+      if (s_bad) atomicExch(err, 1);
+      part[t] = v0;
+    }
   }
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
 }
@@ -1049,7 +1072,10 @@ k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     if (lane == 0) cs[q] = v;
   }
   __syncthreads();
-  if (threadIdx.x == 0) part[t] = tile_total(cs, nc);
+  if (threadIdx.x < 32) {
+    double v0 = tile_total(cs, nc);
+    if (threadIdx.x == 0) part[t] = v0;
+  }
 }
 
 // Tridiagonal eigensolve for the Ritz vector, one warp per group.
@@ -1318,7 +1344,7 @@ struct Lanczos {
     T = (int)hb.size();
     ll max_tile = 0;
     for (int g = 0; g < A; g++) max_tile = std::max(max_tile, std::min(tile_rows(gn[g]), gn[g]));
-    pr_bd = vec_threads<VT>(max_tile, 2);
+    pr_bd = vec_threads<VT>(max_tile, PR_U);
     ritz_bd = vec_threads<VT>(max_tile, 1);
     VS = (N + 63) & ~(ll)63;
     gs.ensure(A);
