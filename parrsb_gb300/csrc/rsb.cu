@@ -1311,7 +1311,7 @@ struct Lanczos {
   std::vector<cudaEvent_t> ev;  // SpMV start/stop events (timing mode)
   std::vector<cudaEvent_t> evk; // p / r per step, then init, eig, ritz (timing mode)
   int bd = 256;                  // threads per tile block (autotuned per level)
-  int sp_kind = 0;               // SpMV variant: 0 k_spmv, 1 k_spmv_tma (autotuned)
+  int sp_kind = 0;               // SpMV variant (autotuned): 0 k_spmv, 1 k_spmv_tma
   DBuf<int> err;                 // [0]: a staged-SpMV wait gave up
   int pr_bd = 256;               // threads per block of k_pr
   int ritz_bd = 256;             // threads per block of k_ritz

@@ -233,3 +233,4 @@ def test_rsb_staged_spmv_bitwise(monkeypatch, shape, nparts):
     monkeypatch.setenv("PARRSB_GPU_SPMV", "1")
     b = P.part_mesh(vtx, xyz, nparts, partitioner=0)
     np.testing.assert_array_equal(a, b)
+
