@@ -193,6 +193,27 @@ PARRSB_API int parrsb_part_quality(double *q, const int *part, const long long *
 /* Release the device workspace cached by earlier calls on this thread. */
 PARRSB_API void parrsb_gpu_finalize(void);
 
+/* RCB partition (same result as parrsb_part_mesh with partitioner = 1) of a
+ * mesh of at most 8192 elements that allocates nothing: no cudaMalloc /
+ * cudaFree and no allocating library call.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory during the
+ * call: their device memory comes from their own pool or arena, or a
+ * long-running loop must not grow or fragment the device heap.  Every
+ * intermediate lives in one fixed file-scope device array (about 512 KB per
+ * device).
+ *   d_part  device int[nel], written;  d_xyz device double[nel][nv][ndim]
+ *   stream  cudaStream_t to run on (NULL: the legacy default stream); the
+ *           result is ready when the stream reaches it (no synchronisation).
+ * Returns PARRSB_ERR_UNSUPPORTED for nel > 8192 (nothing is launched),
+ * PARRSB_ERR_ARGS for bad arguments, PARRSB_ERR_CUDA for a launch error.
+ * The first call on a device (nel = 0 does only this) resolves the scratch
+ * address and sets a kernel attribute; make it before any stream capture.
+ * The scratch is shared by every call on a device: calls that overlap in
+ * time (other streams, other threads) race on it and must be serialised by
+ * the caller. */
+PARRSB_API int parrsb_part_mesh_rcb_noalloc(int *d_part, const double *d_xyz, int nel, int nv,
+                                            int nparts, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

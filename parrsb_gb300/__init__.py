@@ -29,7 +29,8 @@ EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
            "fparrsb_conn_mesh", "parrsb_part_mesh_device",
            "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
            "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq",
-           "parrsb_read_mesh", "parrsb_dump_con", "parrsb_dump_map"]
+           "parrsb_read_mesh", "parrsb_dump_con", "parrsb_dump_map",
+           "parrsb_part_mesh_rcb_noalloc"]
 
 
 class ParrsbError(RuntimeError):
@@ -110,6 +111,8 @@ def library(build_if_missing=False):
     L.parrsb_dump_map.argtypes = [ctypes.c_char_p, ctypes.c_uint, ctypes.c_uint, P, P]
     L.parrsb_gpu_finalize.argtypes = []
     L.parrsb_gpu_finalize.restype = None
+    L.parrsb_part_mesh_rcb_noalloc.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
+    L.parrsb_part_mesh_rcb_noalloc.restype = ctypes.c_int
     _lib = L
     return L
 

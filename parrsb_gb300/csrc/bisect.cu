@@ -790,6 +790,30 @@ void seg_tree_reduce(const int *perm, const double *cent, ll N, SegTable &t,
 
 }  // namespace
 
+int rcb_small_max() { return SMALL_MAX; }
+
+cudaError_t rcb_small_prepare() {
+  cudaError_t e = cudaFuncSetAttribute(k_rcb_small<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)small_smem_bytes());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_rcb_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)small_smem_bytes());
+}
+
+cudaError_t rcb_small_launch(int *perm, const u32 *rank, const double *uniq, ll N, int ndim,
+                             const ll *seg_start, const ll *seg_n, const int *seg_p,
+                             const int *seg_r0, ll nseg, bool local, int *part,
+                             cudaStream_t stream) {
+  if (local)
+    k_rcb_small<true><<<(unsigned)nseg, SMALL_THREADS, small_smem_bytes(), stream>>>(
+        perm, rank, uniq, N, ndim, seg_start, seg_n, seg_p, seg_r0, part);
+  else
+    k_rcb_small<false><<<(unsigned)nseg, SMALL_THREADS, small_smem_bytes(), stream>>>(
+        perm, rank, uniq, N, ndim, seg_start, seg_n, seg_p, seg_r0, part);
+  return cudaGetLastError();
+}
+
 void compute_centroids(const double *xyz, int nel, int nv, double *cent) {
   int ndim = (nv == 8) ? 3 : 2;
   k_centroids<<<grid_for(nel, 256), 256, 0, ctx().stream>>>(xyz, nel, nv, ndim, cent);

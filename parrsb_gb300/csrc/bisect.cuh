@@ -12,6 +12,19 @@ void compute_centroids(const double *xyz, int nel, int nv, double *cent);
 
 enum BisectKind { BISECT_RCB = 0, BISECT_RIB = 1 };
 
+// The CTA-per-segment RCB recursion on its own, for callers that manage
+// every buffer themselves (no allocation, no library stream).  rank / uniq:
+// ndim x N order-preserving coordinate ranks (equal values -> equal rank)
+// and the coordinate value of each rank; segments of at most rcb_small_max()
+// elements.  rcb_small_prepare() sets the kernels' shared-memory limit on the
+// current device (once per device, before the first launch).
+int rcb_small_max();
+cudaError_t rcb_small_prepare();
+cudaError_t rcb_small_launch(int *perm, const u32 *rank, const double *uniq, ll N, int ndim,
+                             const ll *seg_start, const ll *seg_n, const int *seg_p,
+                             const int *seg_r0, ll nseg, bool local, int *part,
+                             cudaStream_t stream);
+
 struct BisectWs {
   SortWs sort;
   DBuf<u64> keys;
