@@ -267,8 +267,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    if args.fp32 is not None:
-        os.environ["PARRSB_GPU_FP32"] = str(args.fp32)
+    # the named method: FP32 vectors on exact integer weights, FP64 dots and
+    # eigensolve (--fp32 0 runs every vector in FP64)
+    os.environ["PARRSB_GPU_FP32"] = str(1 if args.fp32 is None else args.fp32)
     os.environ.setdefault("PARRSB_VERBOSE_LEVEL", "0")
     import parrsb_gb300 as P
     from parrsb_gb300 import meshgen
@@ -320,21 +321,25 @@ def main():
 
     for _ in range(args.warmup):
         step_device()
-    # ---- timed region (device-resident inputs)
-    os.environ["PARRSB_GPU_TIMING"] = "1"
+    # ---- timed region (device-resident inputs, no per-launch events)
+    os.environ["PARRSB_GPU_TIMING"] = "0"
     clocks = ClockSampler(local)
     clocks.start()
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    stats = []
+    timed = []
     for _ in range(args.steps):
-        stats.append(step_device())
+        timed.append(step_device())
     ev1.record()
     barrier()
     clock_info = clocks.stop()
-    os.environ["PARRSB_GPU_TIMING"] = "0"
     t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3 / args.steps)
+    # ---- one more step with CUDA events around every SpMV and vector update
+    # of the Lanczos graphs (per-kernel times for the roofline and breakdown)
+    os.environ["PARRSB_GPU_TIMING"] = "1"
+    stats = [step_device()]
+    os.environ["PARRSB_GPU_TIMING"] = "0"
     # ---- end to end (host buffers, copies inside the timed region)
     t_e2e = None
     if not args.no_e2e:
@@ -362,6 +367,23 @@ def main():
                  "lanczos_steps": int(sp.lanczos_iters),
                  "kernel_launches": int(sp.kernel_launches)}
         os.environ["PARRSB_GPU_BATCHED"] = "1"
+
+    # ---- the same step with FP64 vectors: time and the error of the mixed path
+    fp64 = None
+    if not args.no_plain and os.environ["PARRSB_GPU_FP32"] == "1":
+        os.environ["PARRSB_GPU_FP32"] = "0"
+        step_device()  # warm-up of the FP64 kernels
+        barrier()
+        tf0 = time.perf_counter()
+        s64 = step_device()
+        barrier()
+        t64 = max_over_ranks(time.perf_counter() - tf0)
+        q64 = P.part_quality(d_part.cpu().numpy(), vtx, nparts)
+        fp64 = {"value": t64, "unit": "s", "what": "one step, every Lanczos vector in FP64",
+                "weighted_cut": q64[0], "imbalance": q64[5],
+                "cut_mixed_over_fp64": q[0] / q64[0] if q64[0] else None,
+                "max_fiedler_resid": s64.max_fiedler_resid}
+        os.environ["PARRSB_GPU_FP32"] = "1"
 
     extras = None
     if not args.no_extras and rank == 0:
@@ -409,12 +431,15 @@ def main():
                      "traffic": tr_val, "kernel": "k_spmv (sliced-ELL Laplacian)",
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "spmv_ms_per_launch": spmv_ms / spmv_launches if spmv_launches else None,
+                     "timed_on": "one step after the timed region, CUDA events around every "
+                                 "SpMV launch inside the Lanczos graphs",
                      "algorithmic_bytes_per_launch": per_launch_bytes},
         "cpu_baseline": cpu,
         "plain_gpu": plain,
+        "fp64_gpu": fp64,
         "other_rows": extras,
         "clocks": clock_info,
-        "gpu_launches": int(sum(x.kernel_launches for x in stats)),
+        "gpu_launches": int(sum(x.kernel_launches for x in timed)),
         "elements_per_s": nel / t_dev,
         "quality": {"weighted_cut": q[0], "cut_pairs": q[1], "imbalance": q[5],
                     "comm_volume": q[6]},

@@ -630,9 +630,11 @@ __device__ __forceinline__ double LaneSum<double>::chunk() const { return warp_t
 //   TM_R: V[it+1] = V[it] - alpha w; tile partial of sum V[it+1]^2
 // The chunk decomposition (32 R rows, aligned to multiples of 32 R) does not
 // depend on the CTA size.  The last tile block of a group finalises it.
-constexpr int PR_U = 4;  // chunks per warp in flight in k_pr
+// k_pr: PR_U chunks per warp in flight on big levels (at least PR_BIG rows),
+// one chunk per warp on smaller ones so that enough warps fill the GPU
+constexpr ll PR_BIG = 1ll << 22;
 
-template <typename VT, int MODE>
+template <typename VT, int MODE, int PR_U>
 __global__ void __launch_bounds__(512)
 k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
      GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
@@ -1092,23 +1094,34 @@ k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
 // orientation).  Writes coef[j] = y_j / |r_j|.
 
 // number of eigenvalues of T below x (Sturm sequence of the leading
-// principal minors, rescaled by powers of two to stay in range)
+// principal minors).  Only the two multiplies and the subtraction of each
+// step use the FP64 pipe (GB300 runs FP64 at 1/64 of the FP32 rate): signs,
+// zero tests and the range check read the bit pattern with integer
+// instructions, and the rescaling multiplies by exact powers of two.
 __device__ __forceinline__ int sturm_count(const double *d, const double *e2, int n, double x) {
+  const double TINY = 1e-300;
   double pm = 1.0, p = __dsub_rn(d[0], x);
-  int cnt = 0;
-  if (p == 0.0) p = -1e-300;
-  if (p < 0.0) cnt++;
+  long long pb = __double_as_longlong(p);
+  if ((pb << 1) == 0) p = -TINY, pb = __double_as_longlong(p);
+  int cnt = pb < 0;
   for (int i = 1; i < n; i++) {
     double pn = fma(__dsub_rn(d[i], x), p, -__dmul_rn(e2[i - 1], pm));
-    if (pn == 0.0) pn = (p > 0.0) ? -1e-300 : 1e-300;  // sign opposite to p
-    if ((pn < 0.0) != (p < 0.0)) cnt++;
+    long long nb = __double_as_longlong(pn);
+    if ((nb << 1) == 0) {  // exact zero: sign opposite to p
+      pn = pb < 0 ? TINY : -TINY;
+      nb = __double_as_longlong(pn);
+    }
+    cnt += (nb ^ pb) < 0;
     pm = p;
     p = pn;
-    double ap = fabs(p);
-    if (ap > 1e200) {
-      p = __dmul_rn(p, 1e-200), pm = __dmul_rn(pm, 1e-200);
-    } else if (ap < 1e-200) {
-      p = __dmul_rn(p, 1e200), pm = __dmul_rn(pm, 1e200);
+    pb = nb;
+    const int ex = (int)((nb >> 52) & 0x7FF);
+    if (ex > 1023 + 600) {
+      p = __dmul_rn(p, 0x1p-600), pm = __dmul_rn(pm, 0x1p-600);
+      pb = __double_as_longlong(p);
+    } else if (ex < 1023 - 600) {
+      p = __dmul_rn(p, 0x1p600), pm = __dmul_rn(pm, 0x1p600);
+      pb = __double_as_longlong(p);
     }
   }
   return cnt;
@@ -1314,6 +1327,7 @@ struct Lanczos {
   int sp_kind = 0;               // SpMV variant (autotuned): 0 k_spmv, 1 k_spmv_tma
   DBuf<int> err;                 // [0]: a staged-SpMV wait gave up
   int pr_bd = 256;               // threads per block of k_pr
+  int pr_u = 4;                  // chunks per warp in flight in k_pr
   int ritz_bd = 256;             // threads per block of k_ritz
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
 
@@ -1344,7 +1358,8 @@ struct Lanczos {
     T = (int)hb.size();
     ll max_tile = 0;
     for (int g = 0; g < A; g++) max_tile = std::max(max_tile, std::min(tile_rows(gn[g]), gn[g]));
-    pr_bd = vec_threads<VT>(max_tile, PR_U);
+    pr_u = N >= PR_BIG ? 4 : 1;
+    pr_bd = vec_threads<VT>(max_tile, pr_u);
     ritz_bd = vec_threads<VT>(max_tile, 1);
     VS = (N + 63) & ~(ll)63;
     gs.ensure(A);
@@ -1428,8 +1443,8 @@ struct Lanczos {
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
       mark(4 * it + 0);
-      k_pr<VT, TM_P><<<T, pr_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS,
-                                          part.p, fargs(it, tol, mpass));
+      (pr_u == 4 ? k_pr<VT, TM_P, 4> : k_pr<VT, TM_P, 1>)<<<T, pr_bd, 0, st>>>(
+          tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
       CK_LAUNCH();
       mark(4 * it + 1);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
@@ -1437,8 +1452,8 @@ struct Lanczos {
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       mark(4 * it + 2);
-      k_pr<VT, TM_R><<<T, pr_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS,
-                                          part.p, fargs(it, tol, mpass));
+      (pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>)<<<T, pr_bd, 0, st>>>(
+          tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
       CK_LAUNCH();
       mark(4 * it + 3);
     }
@@ -1487,7 +1502,10 @@ struct Lanczos {
     const char *force_env = getenv("PARRSB_GPU_SPMV");
     const int force_kind = force_env ? atoi(force_env) : -1;
     static thread_local std::vector<std::pair<std::array<ll, 5>, int>> cache;
-    std::array<ll, 5> key = {(ll)T, (ll)A, N, (ll)lv.max_w, (ll)force_kind};
+    // PARRSB_GPU_SPMV_THREADS: only this block size (128, 256 or 512)
+    const char *th_env = getenv("PARRSB_GPU_SPMV_THREADS");
+    const int force_th = th_env ? atoi(th_env) : 0;
+    std::array<ll, 5> key = {(ll)T, (ll)A, N, (ll)lv.max_w, (ll)force_kind * 1024 + force_th};
     for (auto &kv : cache)
       if (kv.first == key) {
         sp_kind = kv.second >> 16;
@@ -1503,6 +1521,7 @@ struct Lanczos {
     }
     std::vector<std::pair<int, int>> cand;
     for (int th : {128, 256, 512}) {
+      if (force_th && th != force_th) continue;
       if (force_kind < 0 || force_kind == 0) cand.push_back({0, th});
       if ((force_kind < 0 || force_kind == 1) && sp_tma_ok(lv, th)) cand.push_back({1, th});
     }
@@ -1527,6 +1546,9 @@ struct Lanczos {
     sp_kind = pick.first;
     bd = pick.second;
     cache.push_back({key, (pick.first << 16) | pick.second});
+    if (getenv("PARRSB_GPU_AUTOTUNE_LOG"))
+      fprintf(stderr, "parrsb_gb300: SpMV autotune tiles=%d groups=%d rows=%lld -> %s x %d\n", T,
+              A, (long long)N, pick.first ? "k_spmv_tma" : "k_spmv", pick.second);
   }
 
   // Runs all passes; f holds the normalised Fiedler vectors afterwards.
