@@ -122,13 +122,19 @@ def load_peaks():
 
 
 def load_traffic():
-    """DRAM bytes per SpMV launch from the committed ncu summary, scaled to
-    the benchmark's matrix size (see profiles/)."""
+    """DRAM bytes per algorithmic byte of one SpMV launch, from the committed
+    ncu summary of a smaller case (the benchmark's launches are scaled by
+    their own algorithmic bytes: traffic grows with the matrix)."""
+    path = os.path.join(ROOT, "profiles", "k_spmv_rsb_hex_128x128x64_level0.md")
     try:
-        with open(os.path.join(ROOT, "profiles", "spmv_traffic.json")) as f:
-            return json.load(f)
+        with open(path) as f:
+            for line in f:
+                if line.startswith("| dram_bytes_per_algorithmic_byte |"):
+                    return {"dram_bytes_per_algorithmic_byte": float(line.split("|")[2]),
+                            "source": os.path.relpath(path, ROOT)}
     except (OSError, ValueError):
-        return None
+        pass
+    return None
 
 
 def cpu_sample_seconds(shape, nparts):
@@ -429,6 +435,11 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": tr_val, "kernel": "k_spmv (sliced-ELL Laplacian)",
+                     "traffic_note": ("DRAM bytes per launch: ncu dram bytes / algorithmic "
+                                      "bytes of one level-0 launch on the 1M-element box "
+                                      f"({traffic['dram_bytes_per_algorithmic_byte']:.3f}, "
+                                      f"{traffic['source']}) x this launch's algorithmic "
+                                      "bytes") if traffic else None,
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "spmv_ms_per_launch": spmv_ms / spmv_launches if spmv_launches else None,
                      "timed_on": "one step after the timed region, CUDA events around every "
