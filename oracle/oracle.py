@@ -50,6 +50,9 @@ def lib():
                                        ctypes.c_int, ctypes.POINTER(RsbInfo)]
         L.oracle_conn_mesh.argtypes = [P, P, ctypes.c_uint, ctypes.c_uint,
                                        ctypes.c_double, ctypes.c_int, P, P]
+        L.oracle_conn_mesh_periodic.argtypes = [P, P, ctypes.c_uint, ctypes.c_uint,
+                                                ctypes.c_double, ctypes.c_int, P,
+                                                ctypes.c_int, P, P]
         L.oracle_centroids.argtypes = [P, P, ctypes.c_int, ctypes.c_int]
         L.oracle_tree_sum.argtypes = [P, ctypes.c_longlong]
         L.oracle_tree_sum.restype = ctypes.c_double
@@ -88,17 +91,21 @@ def part_mesh(vtx, xyz, nparts, want_order=False, **opts):
     return rc, part, order, info, o
 
 
-def conn_mesh(coord, ndim, tol=0.2, heapsort=False):
-    """Oracle parrsb_conn_mesh.  Returns (rc, vtx, ids, nseg)."""
+def conn_mesh(coord, ndim, tol=0.2, heapsort=False, periodic=None):
+    """Oracle parrsb_conn_mesh.  periodic: optional (n, 4) face records.
+    Returns (rc, vtx, ids, nseg); ids are the ids before periodic matching,
+    nseg the number of distinct ids after it."""
     coord = np.ascontiguousarray(coord, np.float64)
     nv = 4 if ndim == 2 else 8
     nel = coord.size // (nv * ndim)
     vtx = np.zeros(nel * nv, np.int64)
     ids = np.zeros(nel * nv, np.int64)
     nseg = ctypes.c_longlong(0)
-    rc = lib().oracle_conn_mesh(_p(vtx), _p(coord), nel, ndim, tol,
-                                1 if heapsort else 0, _p(ids),
-                                ctypes.byref(nseg))
+    pinfo = None if periodic is None else np.ascontiguousarray(periodic, np.int64)
+    npf = 0 if pinfo is None else len(pinfo)
+    rc = lib().oracle_conn_mesh_periodic(_p(vtx), _p(coord), nel, ndim, tol,
+                                         1 if heapsort else 0, _p(pinfo), npf, _p(ids),
+                                         ctypes.byref(nseg))
     return rc, vtx.reshape(nel, nv), ids.reshape(nel, nv), nseg.value
 
 

@@ -1089,10 +1089,134 @@ static int face_check(const ll *ids, ll nel, int ndim) {
   return err;
 }
 
-int oracle_conn_mesh(long long *vtx, const double *coord, unsigned int nelt,
-                     unsigned ndim, double tol, int heapsort_mode,
-                     long long *ids_out, long long *nseg_out) {
+/* match_periodic_faces (src/con-periodic.c:245-288) on one rank.
+ * pinfo: npinfo records (element, face, partner element, partner face),
+ * 1-based, preprocessor face numbering (src/con.c:38-46).  ids: 0-based ids
+ * of the points in sequence order, renumbered in place.  Returns 0,
+ * PARRSB_ERR_ARGS for a record out of range, PARRSB_ERR_CHECK when paired
+ * faces do not coincide (the reference exits the process there). */
+static const int PRE_TO_SYM_FACE[6] = {2, 1, 3, 0, 4, 5};
+
+typedef struct {
+  ll elem, face, bc0, bc1, idx;
+} bface_t;
+
+static int cmp_bface_elem(const void *a, const void *b) {
+  const bface_t *x = (const bface_t *)a, *y = (const bface_t *)b;
+  if (x->elem != y->elem) return x->elem < y->elem ? -1 : 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx); /* stable */
+}
+
+static int match_periodic(ll *ids, double *const x[3], ll nelt, int ndim, ll nids,
+                          const long long *pinfo, int npinfo, ll *nseg_out) {
+  int nv = ndim == 3 ? 8 : 4, nvf = nv / 2, nfaces = ndim == 3 ? 6 : 4;
+  ll np = nelt * nv;
+  bface_t *b = (bface_t *)malloc((size_t)(npinfo + 1) * sizeof(bface_t));
+  for (int i = 0; i < npinfo; i++) {
+    ll e = pinfo[4 * i] - 1, f = pinfo[4 * i + 1] - 1;
+    ll be = pinfo[4 * i + 2] - 1, bf = pinfo[4 * i + 3] - 1;
+    if (e < 0 || e >= nelt || f < 0 || f >= nfaces || be < 0 || be >= nelt || bf < 0 ||
+        bf >= nfaces) {
+      free(b);
+      return PARRSB_ERR_ARGS;
+    }
+    b[i].elem = e, b[i].face = PRE_TO_SYM_FACE[f];
+    b[i].bc0 = be, b[i].bc1 = PRE_TO_SYM_FACE[bf], b[i].idx = i;
+  }
+  /* setPeriodicFaceCoordinates sorts the boundary array by elementId */
+  qsort(b, (size_t)npinfo, sizeof(bface_t), cmp_bface_elem);
+  /* findConnectedPeriodicFaces / findConnectedPeriodicPairs (:104-170) */
+  ll cap = 16, nm = 0;
+  ll *mmin = (ll *)malloc((size_t)cap * sizeof(ll)), *mmax = (ll *)malloc((size_t)cap * sizeof(ll));
+  int err = 0;
+  for (int i = 0; i < npinfo - 1 && !err; i++)
+    for (int j = i + 1; j < npinfo && !err; j++) {
+      if (b[j].bc0 != b[i].elem || b[j].bc1 != b[i].face) continue;
+      double fx[4][3], gx[4][3];
+      ll fid[4], gid[4];
+      for (int q = 0; q < nvf; q++) {
+        int cf = (ndim == 3 ? FACES3D[b[i].face][q] : FACES2D[b[i].face][q]) - 1;
+        int cg = (ndim == 3 ? FACES3D[b[j].face][q] : FACES2D[b[j].face][q]) - 1;
+        ll pf = b[i].elem * nv + cf, pg = b[j].elem * nv + cg;
+        fid[q] = ids[pf], gid[q] = ids[pg];
+        for (int d = 0; d < ndim; d++) fx[q][d] = x[d][pf], gx[q][d] = x[d][pg];
+      }
+      double fMax = 0.0, gMax = 0.0;
+      for (int d = 0; d < ndim; d++) {
+        double meanF = 0.0, meanG = 0.0;
+        for (int q = 0; q < nvf; q++) {
+          fMax = fMax > fabs(fx[q][d]) ? fMax : fabs(fx[q][d]);
+          gMax = gMax > fabs(gx[q][d]) ? gMax : fabs(gx[q][d]);
+          meanF += fx[q][d];
+          meanG += gx[q][d];
+        }
+        for (int q = 0; q < nvf; q++) {
+          fx[q][d] -= meanF / nvf;
+          gx[q][d] -= meanG / nvf;
+        }
+      }
+      int shift = 0;
+      double d2Min = 1.e20;
+      for (int s = 0; s < nvf; s++) {
+        double d2 = 0.0;
+        for (int q = 0; q < nvf; q++) {
+          int k = nvf - 1 - (q + s) % nvf;
+          double dd = diff_sqr(fx[q][0], gx[k][0]) + diff_sqr(fx[q][1], gx[k][1]);
+          if (ndim == 3) dd = dd + diff_sqr(fx[q][2], gx[k][2]);
+          d2 += dd;
+        }
+        if (d2 < d2Min) d2Min = d2, shift = s;
+      }
+      double fg = fMax > gMax ? fMax : gMax;
+      if (sqrt(d2Min) > 1e-3 * fg) {
+        err = PARRSB_ERR_CHECK;
+        break;
+      }
+      for (int q = 0; q < nvf; q++) {
+        int k = nvf - 1 - (q + shift) % nvf;
+        if (nm == cap) {
+          cap *= 2;
+          mmin = (ll *)realloc(mmin, (size_t)cap * sizeof(ll));
+          mmax = (ll *)realloc(mmax, (size_t)cap * sizeof(ll));
+        }
+        mmin[nm] = fid[q] < gid[k] ? fid[q] : gid[k];
+        mmax[nm] = fid[q] < gid[k] ? gid[k] : fid[q];
+        nm++;
+      }
+    }
+  if (!err) {
+    /* renumberPeriodicVertices (:64-102): repeat min over the pairs until
+     * nothing changes; every id ends at the smallest id of its class */
+    ll *lab = (ll *)malloc((size_t)(nids + 1) * sizeof(ll));
+    for (ll v = 0; v < nids; v++) lab[v] = v;
+    int changed = 1;
+    while (changed) {
+      changed = 0;
+      for (ll t = 0; t < nm; t++) {
+        ll a = lab[mmin[t]], c = lab[mmax[t]];
+        ll m = a < c ? a : c;
+        if (lab[mmin[t]] != m) lab[mmin[t]] = m, changed = 1;
+        if (lab[mmax[t]] != m) lab[mmax[t]] = m, changed = 1;
+      }
+    }
+    /* compressPeriodicVertices (:24-55): consecutive in increasing order */
+    ll *rank = (ll *)malloc((size_t)(nids + 1) * sizeof(ll));
+    ll nroot = 0;
+    for (ll v = 0; v < nids; v++) rank[v] = (lab[v] == v) ? nroot++ : -1;
+    for (ll p = 0; p < np; p++) ids[p] = rank[lab[ids[p]]];
+    if (nseg_out) *nseg_out = nroot;
+    free(lab), free(rank);
+  }
+  free(b), free(mmin), free(mmax);
+  return err;
+}
+
+int oracle_conn_mesh_periodic(long long *vtx, const double *coord, unsigned int nelt,
+                              unsigned ndim, double tol, int heapsort_mode,
+                              const long long *pinfo, int npinfo, long long *ids_out,
+                              long long *nseg_out) {
   if (ndim < 2 || ndim > 3) return PARRSB_ERR_ARGS;
+  if (npinfo < 0 || (npinfo > 0 && !pinfo)) return PARRSB_ERR_ARGS;
   int nv = (ndim == 2) ? 4 : 8;
   ll np = (ll)nelt * nv;
   if (np == 0) {
@@ -1166,11 +1290,23 @@ int oracle_conn_mesh(long long *vtx, const double *coord, unsigned int nelt,
   if (ids_out) memcpy(ids_out, ids, (size_t)np * sizeof(ll));
   int err = element_check(ids, nelt, nv);
   if (!err) err = face_check(ids, nelt, ndim);
+  if (!err) {
+    ll nseg2 = cnt + 1;
+    err = match_periodic(ids, x, nelt, (int)ndim, cnt + 1, pinfo, npinfo, &nseg2);
+    if (!err && nseg_out) *nseg_out = nseg2;
+  }
   if (!err && vtx)
     for (ll p = 0; p < np; p++) vtx[p] = ids[p] + 1;
   for (int d = 0; d < 3; d++) free(x[d]);
   free(dx), free(ord), free(tmp), free(flag), free(ids);
-  return err ? 1 : PARRSB_OK;
+  return err;
+}
+
+int oracle_conn_mesh(long long *vtx, const double *coord, unsigned int nelt,
+                     unsigned ndim, double tol, int heapsort_mode,
+                     long long *ids_out, long long *nseg_out) {
+  return oracle_conn_mesh_periodic(vtx, coord, nelt, ndim, tol, heapsort_mode, NULL, 0,
+                                   ids_out, nseg_out);
 }
 
 /* ------------------------------------------------------------------------ */

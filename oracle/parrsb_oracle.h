@@ -52,6 +52,13 @@ int oracle_part_mesh(int *part, int *order, const long long *vtx,
 int oracle_conn_mesh(long long *vtx, const double *coord, unsigned int nel,
                      unsigned ndim, double tol, int heapsort_mode,
                      long long *ids, long long *nseg);
+/* The same with periodic face records (element, face, partner element,
+ * partner face; 1-based, preprocessor face numbering), matched as
+ * match_periodic_faces does (src/con-periodic.c:245-288). */
+int oracle_conn_mesh_periodic(long long *vtx, const double *coord, unsigned int nel,
+                              unsigned ndim, double tol, int heapsort_mode,
+                              const long long *pinfo, int npinfo, long long *ids,
+                              long long *nseg);
 
 /* Pieces exposed for unit tests. */
 void oracle_centroids(double *cent, const double *xyz, int nel, int nv);

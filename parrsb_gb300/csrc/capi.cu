@@ -15,6 +15,7 @@
 
 #include "bisect.cuh"
 #include "gencon.cuh"
+#include "periodic.cuh"
 #include "rsb.cuh"
 
 extern "C" {
@@ -394,11 +395,10 @@ extern "C" int parrsb_part_mesh_device(int *d_part, const long long *d_vtx, cons
 
 extern "C" int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel, unsigned nDim,
                                 long long *periodicInfo, int nPeriodicFaces, double tol) {
-  (void)periodicInfo;
   int verbose = 1;
   if (const char *v = getenv("PARRSB_VERBOSE_LEVEL")) verbose = atoi(v);
   if (nDim < 2 || nDim > 3) return PARRSB_ERR_ARGS;
-  if (nPeriodicFaces > 0) return PARRSB_ERR_UNSUPPORTED;
+  if (nPeriodicFaces < 0 || (nPeriodicFaces > 0 && !periodicInfo)) return PARRSB_ERR_ARGS;
   if (nel > 0 && (!vtx || !coord)) return PARRSB_ERR_ARGS;
   auto t0 = std::chrono::steady_clock::now();
   print_if(verbose, "Running parCon ...");
@@ -418,12 +418,25 @@ extern "C" int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel,
     int r;
     {
       StageTimer tm(PARRSB_STAGE_GENCON);
-      r = gencon_device(W.ids.p, W.xyz.p, nel, (int)nDim, tol, W.gc, &nseg, nullptr);
+      r = gencon_device(nullptr, W.xyz.p, nel, (int)nDim, tol, W.gc, &nseg, nullptr);
     }
     ctx().stats.gencon_segments = nseg;
     if (r != PARRSB_OK) {
       print_if(1, "\t%s:%d element_check / face_check failed.", __FILE__, __LINE__);
       return r;
+    }
+    {
+      // periodic faces (src/con.c:261-264); without any, the consecutive
+      // renumbering leaves the ids as they are
+      StageTimer tm(PARRSB_STAGE_GENCON);
+      r = periodic_device(W.gc.ids.p, W.gc.x[0].p, W.gc.x[1].p, W.gc.x[2].p, nel, (int)nDim,
+                          nseg, periodicInfo, nPeriodicFaces, W.gc.sort, &nseg);
+      ctx().stats.gencon_segments = nseg;
+      if (r != PARRSB_OK) {
+        print_if(1, "\t%s:%d periodic faces did not match.", __FILE__, __LINE__);
+        return r;
+      }
+      plus_one(W.gc.ids.p, np, W.ids.p);
     }
     {
       StageTimer tm(PARRSB_STAGE_DOWNLOAD);

@@ -61,6 +61,44 @@ def box_hex(nx, ny, nz, jitter=0.1, seed=0, lo=(0.0, 0.0, 0.0),
     return np.ascontiguousarray(vtx), np.ascontiguousarray(xyz)
 
 
+def box_quad(nx, ny, jitter=0.1, seed=0):
+    """2D quad box on [0, 1]^2 with uniform jitter of +-jitter*h on interior
+    lattice vertices.  Returns (vtx[nel,4] int64, xyz[nel,4,2]); elements
+    are x-fastest."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    h = np.array([1.0 / nx, 1.0 / ny])
+    X = np.empty((ny + 1, nx + 1, 2), np.float64)
+    X[..., 0] = (np.arange(nx + 1, dtype=np.float64) * h[0])[None, :]
+    X[..., 1] = (np.arange(ny + 1, dtype=np.float64) * h[1])[:, None]
+    if jitter:
+        J = _uniform_pm1(rng, (ny - 1, nx - 1, 2))
+        X[1:ny, 1:nx, :] = X[1:ny, 1:nx, :] + J * np.asarray(jitter * h, np.float64)
+    j, i = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    base = np.stack([i.ravel(), j.ravel()], axis=1)
+    c = base[:, None, :] + QUAD_CORNERS[None, :, :]
+    xyz = X[c[..., 1], c[..., 0]]
+    vid = c[..., 0] + (nx + 1) * c[..., 1]
+    return np.ascontiguousarray((vid + 1).astype(np.int64)), np.ascontiguousarray(xyz)
+
+
+def periodic_x_faces(nx, ny, nz=None, both=True):
+    """Periodic face records (element, face, partner element, partner face;
+    1-based, preprocessor face numbers 4 = x-low, 2 = x-high) joining the
+    x = 0 and x = 1 sides of box_hex(nx, ny, nz) or, with nz None, of
+    box_quad(nx, ny).  both: list every pair from both sides, as Nek's .re2
+    boundary section does."""
+    layers = 1 if nz is None else nz
+    out = []
+    for k in range(layers):
+        for j in range(ny):
+            lo = 1 + nx * (j + ny * k)
+            hi = lo + nx - 1
+            out.append((lo, 4, hi, 2))
+            if both:
+                out.append((hi, 2, lo, 4))
+    return np.array(out, dtype=np.int64).reshape(-1, 4)
+
+
 def annulus_quad(nt, nr, amp=0.02, seed=0):
     """2D quad annulus r in [1, 2]: nt elements around, nr across.  The
     radius carries a seeded sinusoidal perturbation of amplitude `amp`

@@ -133,13 +133,15 @@ def test_conn_mesh_argument_checks(lib):
     coord = np.zeros(8 * 3, np.float64)
     vtx = np.zeros(8, np.int64)
     assert lib.parrsb_conn_mesh(P_(vtx), P_(coord), 1, 4, None, 0, 0.2) == 1
+    # periodic records: a negative count, or a count without records
     pinfo = np.ones(4, np.int64)
-    assert lib.parrsb_conn_mesh(P_(vtx), P_(coord), 1, 3, P_(pinfo), 1, 0.2) == 4
+    assert lib.parrsb_conn_mesh(P_(vtx), P_(coord), 1, 3, P_(pinfo), -1, 0.2) == 1
+    assert lib.parrsb_conn_mesh(P_(vtx), P_(coord), 1, 3, None, 1, 0.2) == 1
     err = ctypes.c_int(0)
     nel, nd, npf, tol = ctypes.c_int(1), ctypes.c_int(3), ctypes.c_int(1), ctypes.c_double(0.2)
     lib.fparrsb_conn_mesh(P_(vtx), P_(coord), ctypes.byref(nel), ctypes.byref(nd),
-                          P_(pinfo), ctypes.byref(npf), ctypes.byref(tol), ctypes.byref(err))
-    assert err.value == 4
+                          None, ctypes.byref(npf), ctypes.byref(tol), ctypes.byref(err))
+    assert err.value == 1
 
 
 def test_quality_rejects_out_of_range_parts(lib):

@@ -234,3 +234,41 @@ def test_rsb_staged_spmv_bitwise(monkeypatch, shape, nparts):
     b = P.part_mesh(vtx, xyz, nparts, partitioner=0)
     np.testing.assert_array_equal(a, b)
 
+
+
+# -------------------------------------------------------- periodic gencon
+@pytest.mark.parametrize("shape", [(5, 4, 3), (32, 24, 16), (7, 1, 1)])
+def test_gencon_periodic_hex_bit_exact(oracle, shape):
+    nx, ny, nz = shape
+    _, xyz = meshgen.box_hex(nx, ny, nz, jitter=0.1, seed=21)
+    pf = meshgen.periodic_x_faces(nx, ny, nz)
+    ids = P.conn_mesh(xyz, 3, 0.2, periodic=pf)
+    rc, ref, _, nseg = oracle.conn_mesh(xyz, 3, 0.2, periodic=pf)
+    assert rc == 0
+    np.testing.assert_array_equal(ids, ref)
+    assert nseg == nx * (ny + 1) * (nz + 1)
+    assert P.last_stats().gencon_segments == nseg
+
+
+def test_gencon_periodic_quad_and_one_sided(oracle):
+    nx, ny = 40, 24
+    _, xyz = meshgen.box_quad(nx, ny, jitter=0.1, seed=22)
+    for pf in (meshgen.periodic_x_faces(nx, ny), meshgen.periodic_x_faces(nx, ny, both=False)):
+        ids = P.conn_mesh(xyz, 2, 0.2, periodic=pf)
+        rc, ref, _, nseg = oracle.conn_mesh(xyz, 2, 0.2, periodic=pf)
+        assert rc == 0
+        np.testing.assert_array_equal(ids, ref)
+        assert P.last_stats().gencon_segments == nseg
+
+
+def test_gencon_periodic_errors(oracle):
+    _, xyz = meshgen.box_hex(5, 4, 3, jitter=0.1, seed=2)
+    with pytest.raises(P.ParrsbError) as ei:
+        P.conn_mesh(xyz, 3, 0.2, periodic=[(1, 4, 99, 2)])
+    assert ei.value.code == 1
+    with pytest.raises(P.ParrsbError) as ei:  # faces that do not coincide
+        P.conn_mesh(xyz, 3, 0.2, periodic=[(1, 4, 27, 2), (27, 2, 1, 4)])
+    assert ei.value.code == 3
+    # the library is usable afterwards
+    ids = P.conn_mesh(xyz, 3, 0.2, periodic=meshgen.periodic_x_faces(5, 4, 3))
+    assert len(np.unique(ids)) == 5 * 5 * 4

@@ -243,3 +243,50 @@ def test_unknown_partitioner_block_distribution(oracle):
     rc, part, _, _, _ = oracle.part_mesh(vtx, xyz, 3, partitioner=7)
     # first nel % p ranks get one more element (src/parrsb.c:112-137)
     assert np.bincount(part).tolist() == [4, 3, 3]
+
+
+# ------------------------------------------------------------- periodic gencon
+def test_oracle_periodic_one_sided_records_pair_nothing(oracle):
+    """A face pairs only with a face that is itself listed
+    (src/con-periodic.c:157-170): records from one side alone merge nothing."""
+    nx, ny, nz = 5, 4, 3
+    _, xyz = meshgen.box_hex(nx, ny, nz, jitter=0.1, seed=2)
+    rc, _, _, nseg = oracle.conn_mesh(xyz, 3, 0.2,
+                                      periodic=meshgen.periodic_x_faces(nx, ny, nz, False))
+    assert rc == 0 and nseg == (nx + 1) * (ny + 1) * (nz + 1)
+
+
+def test_oracle_periodic_box_wraps_x(oracle):
+    """Periodic x faces of a jittered hex box: the x = 0 and x = 1 vertices
+    merge, giving nx (ny + 1)(nz + 1) ids, and every id equals the lattice
+    id with i taken modulo nx."""
+    nx, ny, nz = 5, 4, 3
+    vtx, xyz = meshgen.box_hex(nx, ny, nz, jitter=0.1, seed=2)
+    rc, ids, _, nseg = oracle.conn_mesh(xyz, 3, 0.2,
+                                        periodic=meshgen.periodic_x_faces(nx, ny, nz))
+    assert rc == 0
+    assert nseg == nx * (ny + 1) * (nz + 1)
+    # lattice (i, j, k) of each corner in symmetric order, i wrapped
+    lat = vtx - 1
+    i, rest = lat % (nx + 1), lat // (nx + 1)
+    wrapped = (i % nx) + nx * rest
+    sym = [0, 1, 3, 2, 4, 5, 7, 6]
+    w = wrapped[:, sym]
+    # equal lattice points <-> equal ids
+    pairs = {}
+    for a, b in zip(w.ravel(), ids.ravel()):
+        assert pairs.setdefault(a, b) == b
+    assert len(set(ids.ravel())) == nseg
+
+
+def test_oracle_periodic_quad_and_errors(oracle):
+    nx, ny = 6, 4
+    _, xyz = meshgen.box_quad(nx, ny, jitter=0.1, seed=3)
+    rc, _, _, nseg = oracle.conn_mesh(xyz, 2, 0.2, periodic=meshgen.periodic_x_faces(nx, ny))
+    assert rc == 0 and nseg == nx * (ny + 1)
+    rc, _, _, _ = oracle.conn_mesh(xyz, 2, 0.2, periodic=[(1, 4, 99, 2)])
+    assert rc == 1  # record out of range
+    # an x-low face paired with the x-high face of a jittered interior element
+    _, xyz3 = meshgen.box_hex(5, 4, 3, jitter=0.1, seed=2)
+    rc, _, _, _ = oracle.conn_mesh(xyz3, 3, 0.2, periodic=[(1, 4, 27, 2), (27, 2, 1, 4)])
+    assert rc == 3  # faces do not coincide
