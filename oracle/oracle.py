@@ -109,6 +109,28 @@ def conn_mesh(coord, ndim, tol=0.2, heapsort=False, periodic=None):
     return rc, vtx.reshape(nel, nv), ids.reshape(nel, nv), nseg.value
 
 
+def part_mesh_tagged(vtx, xyz, tag, nparts, **opts):
+    """Oracle of tagged partitioning (parrsb_part_mesh_v1,
+    src/parrsb.c:379-561): tags numbered in increasing order, nparts a
+    multiple of their number; the elements of tag number t, in input order,
+    are partitioned by parrsb_part_mesh_v0 among nparts / ntags ranks, whose
+    part numbers start at t * nparts / ntags.  Returns (rc, part)."""
+    tag = np.asarray(tag)
+    u = np.unique(tag)
+    if nparts % len(u):
+        return 1, None
+    chunk = nparts // len(u)
+    part = np.full(len(tag), -1, np.int32)
+    for t, val in enumerate(u):
+        sel = np.flatnonzero(tag == val)
+        rc, p, _, _, _ = part_mesh(None if vtx is None else vtx[sel],
+                                   None if xyz is None else xyz[sel], chunk, **opts)
+        if rc:
+            return rc, None
+        part[sel] = p + t * chunk
+    return 0, part
+
+
 def centroids(xyz, nv):
     xyz = np.ascontiguousarray(xyz, np.float64)
     nel = xyz.shape[0]

@@ -10,6 +10,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <stdexcept>
 
@@ -144,7 +145,6 @@ int prepare_options(const long long *vtx, const double *xyz, int nel, int nv,
     print_if(o->verbose_level, "Tagged partitioning requested but tag array is NULL..");
     return PARRSB_ERR_ARGS;
   }
-  if (o->tagged == 1) return PARRSB_ERR_UNSUPPORTED;
   if (nel < 0 || nparts < 1 || nv < 1 || nv > 8) return PARRSB_ERR_ARGS;
   if (vtx == nullptr && xyz == nullptr) {
     print_if(o->verbose_level,
@@ -195,7 +195,8 @@ __global__ void k_seq_write(const int *__restrict__ perm, const int *__restrict_
 }
 
 void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int nel, int nv,
-                   const parrsb_options *o, int nparts, int *d_seq = nullptr) {
+                   const parrsb_options *o, int nparts, int *d_seq = nullptr,
+                   const StartGroups *sg = nullptr) {
   cudaStream_t st = ctx().stream;
   if (nel == 0) return;
   int ndim = (nv == 8) ? 3 : 2;
@@ -211,22 +212,33 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     StageTimer tm(PARRSB_STAGE_PRE);
     BisectWs bws;
     DBuf<int> perm((size_t)N);
-    std::vector<int> h(N);
-    for (ll i = 0; i < N; i++) h[i] = (int)i;
-    h2d(perm.p, h.data(), N);
     SegTable t;
-    t.reserve(1);
-    ll s0 = 0, n0 = N;
-    int p0 = P, r00 = 0;
-    h2d(t.start.p, &s0, 1);
-    h2d(t.n.p, &n0, 1);
-    h2d(t.p.p, &p0, 1);
-    h2d(t.r0.p, &r00, 1);
-    t.count = 1;
+    if (sg) {  // tagged: one segment per tag
+      const ll ng = (ll)sg->start.size();
+      h2d(perm.p, sg->perm.data(), N);
+      t.reserve(ng);
+      h2d(t.start.p, sg->start.data(), ng);
+      h2d(t.n.p, sg->n.data(), ng);
+      h2d(t.p.p, sg->p.data(), ng);
+      h2d(t.r0.p, sg->r0.data(), ng);
+      t.count = ng;
+    } else {
+      std::vector<int> h(N);
+      for (ll i = 0; i < N; i++) h[i] = (int)i;
+      h2d(perm.p, h.data(), N);
+      t.reserve(1);
+      ll s0 = 0, n0 = N;
+      int p0 = P, r00 = 0;
+      h2d(t.start.p, &s0, 1);
+      h2d(t.n.p, &n0, 1);
+      h2d(t.p.p, &p0, 1);
+      h2d(t.r0.p, &r00, 1);
+      t.count = 1;
+    }
     bisect_segments(o->partitioner == 1 ? BISECT_RCB : BISECT_RIB, perm, t, W.cent.p, N, ndim,
                     d_seq != nullptr, d_part, bws);
     if (d_seq) {
-      DBuf<int> first((size_t)P);
+      DBuf<int> first((size_t)nparts);
       k_seq_from_order<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
       CK_LAUNCH();
       k_seq_write<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
@@ -245,7 +257,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.check_resid = env_int("PARRSB_GPU_CHECK_RESID", 1);
     ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
     ro.batched = env_int("PARRSB_GPU_BATCHED", 1);
-    rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq);
+    rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq, sg);
     sync();
   } else {
     k_block_part<<<grid_for(N, 256), 256, 0, st>>>(d_part, N, nparts);
@@ -325,6 +337,45 @@ extern "C" int parrsb_part_mesh_seq(int *part, int *seq, const long long *vtx,
   return part_mesh_host(part, seq, vtx, xyz, tag, nel, nv, options, nparts);
 }
 
+// Tagged partitioning (parrsb_part_mesh_v1, src/parrsb.c:379-561): tags are
+// numbered in increasing order; nparts must be a multiple of their number;
+// the elements of tag number t, in input order, are partitioned among the
+// nparts / ntags ranks starting at t * nparts / ntags, independently of the
+// other tags.  Here all tags run in the same launches: the recursion starts
+// from one group per tag.
+static int tagged_groups(const int *tag, int nel, int nparts, int verbose, StartGroups &sg) {
+  std::vector<int> u(tag, tag + nel);
+  std::sort(u.begin(), u.end());
+  u.erase(std::unique(u.begin(), u.end()), u.end());
+  const int ntags = (int)u.size();
+  print_if(verbose, "Num tags: %d", ntags);
+  if (ntags == 0) return PARRSB_OK;
+  if (nparts % ntags != 0) {
+    print_if(1, "Number of processes must be a multiple of number of tags: "
+                "processes = %d, tags = %d.", nparts, ntags);
+    return PARRSB_ERR_ARGS;
+  }
+  const int chunk = nparts / ntags;
+  std::vector<ll> cnt(ntags + 1, 0);
+  std::vector<int> tn(nel);
+  for (int e = 0; e < nel; e++) {
+    tn[e] = (int)(std::lower_bound(u.begin(), u.end(), tag[e]) - u.begin());
+    cnt[tn[e] + 1]++;
+  }
+  for (int t = 0; t < ntags; t++) cnt[t + 1] += cnt[t];
+  sg.perm.assign(nel, 0);
+  std::vector<ll> fill(cnt.begin(), cnt.end() - 1);
+  for (int e = 0; e < nel; e++) sg.perm[fill[tn[e]]++] = e;  // stable: input order
+  for (int t = 0; t < ntags; t++) {
+    const ll n = cnt[t + 1] - cnt[t];
+    sg.start.push_back(cnt[t]);
+    sg.n.push_back(n);
+    sg.p.push_back((int)std::min<ll>(chunk, n));  // fewer elements than ranks
+    sg.r0.push_back(t * chunk);
+  }
+  return PARRSB_OK;
+}
+
 static int part_mesh_host(int *part, int *seq, const long long *vtx, const double *xyz,
                           const int *tag, int nel, int nv, parrsb_options *options,
                           int nparts) {
@@ -332,6 +383,13 @@ static int part_mesh_host(int *part, int *seq, const long long *vtx, const doubl
   int rc = prepare_options(vtx, xyz, nel, nv, options, nparts, tag, true);
   if (rc != PARRSB_OK) return rc;
   if (nel > 0 && !part) return PARRSB_ERR_ARGS;
+  StartGroups sg;
+  const bool tagged = options->tagged == 1 && nel > 0;
+  if (tagged) {
+    if (options->partitioner < 0 || options->partitioner > 2) return PARRSB_ERR_UNSUPPORTED;
+    rc = tagged_groups(tag, nel, nparts, options->verbose_level, sg);
+    if (rc != PARRSB_OK) return rc;
+  }
   rc = guarded([&]() -> int {
     ctx().init();
     Workspace &W = ws();
@@ -354,7 +412,7 @@ static int part_mesh_host(int *part, int *seq, const long long *vtx, const doubl
     DBuf<int> dseq;
     if (seq) dseq.alloc((size_t)N);
     part_mesh_dev(W.part.p, vtx ? W.vtx.p : nullptr, xyz ? W.xyz.p : nullptr, nel, nv, options,
-                  nparts, seq ? dseq.p : nullptr);
+                  nparts, seq ? dseq.p : nullptr, tagged ? &sg : nullptr);
     maybe_fault("partition");
     {
       StageTimer tm(PARRSB_STAGE_DOWNLOAD);

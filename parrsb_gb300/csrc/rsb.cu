@@ -1970,7 +1970,7 @@ void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g, SortWs &
 
 template <typename VT>
 static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, int P,
-                     const RsbOpts &o, int *d_part, int *d_seq) {
+                     const RsbOpts &o, int *d_part, int *d_seq, const StartGroups *sg) {
   cudaStream_t st = ctx().stream;
   int ndim = (nv == 8) ? 3 : 2;
   parrsb_stats &S = ctx().stats;
@@ -1989,12 +1989,17 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
   DBuf<double> f_pos((size_t)N), f_tmp((size_t)N);
   DBuf<u64> keys((size_t)N);
   DBuf<int> vals((size_t)N), perm2((size_t)N);
-  {
+  std::vector<HGroup> groups;
+  if (sg) {
+    h2d(perm.p, sg->perm.data(), N);
+    for (size_t g = 0; g < sg->start.size(); g++)
+      groups.push_back({sg->start[g], sg->n[g], sg->p[g], sg->r0[g]});
+  } else {
     std::vector<int> h(N);
     for (ll i = 0; i < N; i++) h[i] = (int)i;
     h2d(perm.p, h.data(), N);
+    groups.push_back({0, N, P, 0});
   }
-  std::vector<HGroup> groups = {{0, N, P, 0}};
   int ncuts = 0;
   for (ll pw = 1; pw < P; pw <<= 1) ncuts++;
   BisectWs bws;
@@ -2398,13 +2403,13 @@ void fiedler_groups_device(const long long *d_vtx, ll N, int nv, const int *d_gr
 }
 
 void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv, int P,
-                const RsbOpts &o, int *d_part, int *d_seq) {
+                const RsbOpts &o, int *d_part, int *d_seq, const StartGroups *sg) {
   if (o.miter > MAX_MITER || o.miter < 1)
     throw ArgError{PARRSB_ERR_UNSUPPORTED, "rsb_max_iter outside [1, 120]"};
   if (o.fp32)
-    rsb_impl<float>(d_vtx, cent, N, nv, P, o, d_part, d_seq);
+    rsb_impl<float>(d_vtx, cent, N, nv, P, o, d_part, d_seq, sg);
   else
-    rsb_impl<double>(d_vtx, cent, N, nv, P, o, d_part, d_seq);
+    rsb_impl<double>(d_vtx, cent, N, nv, P, o, d_part, d_seq, sg);
 }
 
 }  // namespace prsb

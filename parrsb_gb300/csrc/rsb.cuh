@@ -1,5 +1,6 @@
 // rsb.cuh -- recursive spectral bisection on one GPU.
 #pragma once
+#include <vector>
 #include "bisect.cuh"
 
 namespace prsb {
@@ -30,9 +31,22 @@ struct RsbOpts {
   int batched = 1;      // all groups of a level per launch (0: one group at a time)
 };
 
-// Partition N elements (vertex ids d_vtx, centroids cent) into P parts.
+// Starting point of a recursion other than one group of all elements:
+// tagged partitioning (src/parrsb.c:379-561) starts from one group per tag.
+// perm[i] is the element at position i; group g covers positions
+// [start[g], start[g] + n[g]) and is split among p[g] ranks numbered from
+// r0[g].
+struct StartGroups {
+  std::vector<int> perm;
+  std::vector<ll> start, n;
+  std::vector<int> p, r0;
+};
+
+// Partition N elements (vertex ids d_vtx, centroids cent) into P parts, or,
+// with sg, each start group into its own ranks.
 void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv,
-                int P, const RsbOpts &o, int *d_part, int *d_seq = nullptr);
+                int P, const RsbOpts &o, int *d_part, int *d_seq = nullptr,
+                const StartGroups *sg = nullptr);
 
 // Fiedler vectors of independent element groups: group g is the elements
 // e with group_of[e] == g, taken in element order (that order defines the

@@ -89,11 +89,26 @@ def test_tagged_without_tag_returns_1(lib):
     assert _call(lib, vtx, xyz, 2, o) == 1  # src/parrsb.c:873-877
 
 
-def test_tagged_with_tag_is_unsupported(lib):
+def test_tagged_parts_must_be_a_multiple_of_tags(lib):
+    # the reference exits (src/parrsb.c:431-439); here: code 1, before any GPU work
     vtx, xyz = meshgen.box_hex(2, 2, 2)
     o = ParrsbOptions.make(tagged=1, verbose_level=0)
-    tag = np.zeros(8, np.int32)
-    assert _call(lib, vtx, xyz, 2, o, tag=tag) == P.ERR_UNSUPPORTED
+    tag = np.array([0, 0, 1, 1, 2, 2, 3, 3], np.int32)
+    assert _call(lib, vtx, xyz, 6, o, tag=tag) == 1
+
+
+def test_oracle_tagged_composition(oracle):
+    """Tags are numbered in increasing order and partition independently:
+    tag number t owns parts [t * chunk, (t + 1) * chunk)."""
+    vtx, xyz = meshgen.box_hex(6, 5, 4, jitter=0.1, seed=1)
+    tag = np.repeat(np.array([7, 3, 9, 3]), 30).astype(np.int32)  # z layers
+    rc, part = oracle.part_mesh_tagged(vtx, xyz, tag, 9, partitioner=1)
+    assert rc == 0
+    for t, val in enumerate([3, 7, 9]):
+        got = np.unique(part[tag == val])
+        np.testing.assert_array_equal(got, np.arange(3 * t, 3 * t + 3))
+    rc, _ = oracle.part_mesh_tagged(vtx, xyz, tag, 8, partitioner=1)
+    assert rc == 1  # 8 parts over 3 tags
 
 
 def test_both_inputs_null_is_an_error(lib):

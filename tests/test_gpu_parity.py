@@ -272,3 +272,50 @@ def test_gencon_periodic_errors(oracle):
     # the library is usable afterwards
     ids = P.conn_mesh(xyz, 3, 0.2, periodic=meshgen.periodic_x_faces(5, 4, 3))
     assert len(np.unique(ids)) == 5 * 5 * 4
+
+
+# ------------------------------------------------------ tagged partitioning
+def _layer_tags(nz, per_layer, values):
+    return np.repeat(np.asarray(values)[np.arange(nz) % len(values)], per_layer).astype(np.int32)
+
+
+@pytest.mark.parametrize("partitioner", [1, 2])
+@pytest.mark.parametrize("nparts", [6, 12, 300])
+def test_tagged_bisection_bit_exact(oracle, partitioner, nparts):
+    vtx, xyz = meshgen.box_hex(12, 10, 6, jitter=0.1, seed=31)
+    tag = _layer_tags(6, 120, [5, 2, 8])
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=partitioner, tagged=1, tag=tag)
+    rc, ref = oracle.part_mesh_tagged(vtx, xyz, tag, nparts, partitioner=partitioner)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
+
+
+def test_tagged_rsb_equals_separate_runs(oracle):
+    """All tags run in the same launches; the result is bitwise the one of
+    partitioning every tag's elements on its own, and its cut is within 1%
+    of the oracle's."""
+    vtx, xyz = meshgen.box_hex(16, 12, 8, jitter=0.1, seed=32)
+    tag = _layer_tags(8, 192, [1, 4])
+    nparts = 8
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=0, tagged=1, tag=tag)
+    sep = np.full(len(tag), -1, np.int32)
+    for t, val in enumerate([1, 4]):
+        sel = np.flatnonzero(tag == val)
+        sep[sel] = P.part_mesh(vtx[sel], xyz[sel], 4, partitioner=0) + 4 * t
+    np.testing.assert_array_equal(part, sep)
+    rc, ref = oracle.part_mesh_tagged(vtx, xyz, tag, nparts, partitioner=0)
+    assert rc == 0
+    np.testing.assert_array_equal(np.bincount(part, minlength=nparts),
+                                  np.bincount(ref, minlength=nparts))
+    q, qr = oracle.part_quality(part, vtx, nparts), oracle.part_quality(ref, vtx, nparts)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+
+
+def test_tagged_fewer_elements_than_ranks(oracle):
+    vtx, xyz = meshgen.box_hex(4, 3, 2, jitter=0.1, seed=33)
+    tag = np.zeros(24, np.int32)
+    tag[:3] = 1  # tag 1 has 3 elements for 10 ranks
+    part = P.part_mesh(vtx, xyz, 20, partitioner=1, tagged=1, tag=tag)
+    rc, ref = oracle.part_mesh_tagged(vtx, xyz, tag, 20, partitioner=1)
+    assert rc == 0
+    np.testing.assert_array_equal(part, ref)
