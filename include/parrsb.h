@@ -16,13 +16,18 @@
  * otherwise aborts the process; this library never exits):
  *   PARRSB_OK            0  success
  *   PARRSB_ERR_ARGS      1  bad arguments (also: tagged == 1 with tag NULL,
- *                           as in src/parrsb.c:873-877; gencon: element or
- *                           face check failed, as in src/con.c:238-257)
+ *                           as in src/parrsb.c:873-877; tagged with nparts
+ *                           not a multiple of the number of tags, where the
+ *                           reference exits; gencon: element or face check
+ *                           failed, as in src/con.c:238-257; a periodic face
+ *                           record out of range)
  *   PARRSB_ERR_CUDA      2  a CUDA call failed (message on stderr)
- *   PARRSB_ERR_CHECK     3  an internal consistency check failed
- *   PARRSB_ERR_UNSUPPORTED 4 option outside the GPU path (tagged
- *                           partitioning, rsb_algo = 1 multigrid, periodic
- *                           faces in gencon)
+ *   PARRSB_ERR_CHECK     3  an internal consistency check failed (also:
+ *                           paired periodic faces that do not coincide,
+ *                           where the reference exits)
+ *   PARRSB_ERR_UNSUPPORTED 4 option outside the GPU path (rsb_algo = 1
+ *                           multigrid; tagged with a partitioner other than
+ *                           0, 1, 2)
  */
 #ifndef PARRSB_GB300_H
 #define PARRSB_GB300_H
@@ -49,7 +54,7 @@ extern "C" {
  * update_options (src/parrsb.c:48-77). */
 typedef struct {
   int partitioner;             /* 0 RSB, 1 RCB, 2 RIB (default 0) */
-  int tagged;                  /* tagged partitioning (unsupported here) */
+  int tagged;                  /* tagged partitioning: tag[e] groups elements */
   int levels;                  /* 1 or 2; clamped to <= 2 (default 2) */
   int find_disconnected_comps; /* count components per bisection (1) */
   int repair;                  /* accepted, no effect (as in the reference) */
@@ -73,7 +78,12 @@ extern PARRSB_API parrsb_options parrsb_default_options;
  * Replaces parrsb_part_mesh (src/parRSB.h:45-48, src/parrsb.c:853-906);
  * `comm` becomes `nparts`.  vtx: nel*nv global vertex ids (may be NULL for
  * RCB/RIB); xyz: nel*nv*ndim corner coordinates (may be NULL: rsb_pre is then
- * set to 0, as src/parrsb.c:250 does). */
+ * set to 0, as src/parrsb.c:250 does).  With options->tagged == 1 and a
+ * tag array (parrsb_part_mesh_v1, src/parrsb.c:379-561): nparts must be a
+ * multiple of the number of distinct tags; the elements of the t-th
+ * smallest tag, in input order, are partitioned among nparts / ntags parts
+ * numbered from t * nparts / ntags, independently of the other tags (all
+ * tags run in the same GPU launches). */
 PARRSB_API int parrsb_part_mesh(int *part, const long long *vtx, const double *xyz,
                      const int *tag, int nel, int nv, parrsb_options *options,
                      int nparts);
@@ -82,8 +92,11 @@ PARRSB_API int parrsb_part_mesh(int *part, const long long *vtx, const double *x
  * (src/parRSB.h:62-64, src/con.c:189-295) without the communicator.
  * coord: nel * nv * nDim doubles, corners in Nek preprocessor order;
  * vtx: nel * nv output ids in symmetric corner order (1-based, dense).
- * Returns 1 when the element or face check fails (vtx is then untouched),
- * 4 when nPeriodicFaces > 0. */
+ * periodicInfo: nPeriodicFaces records (element, face, partner element,
+ * partner face), 1-based, faces in preprocessor numbering; paired faces'
+ * corners are merged (match_periodic_faces, src/con-periodic.c:245-288).
+ * Returns 1 when the element or face check fails or a record is out of
+ * range, 3 when paired faces do not coincide (vtx is then untouched). */
 PARRSB_API int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel,
                      unsigned nDim, long long *periodicInfo,
                      int nPeriodicFaces, double tol);
