@@ -321,3 +321,4 @@ def test_tagged_fewer_elements_than_ranks(oracle):
     rc, ref = oracle.part_mesh_tagged(vtx, xyz, tag, 20, partitioner=1)
     assert rc == 0
     np.testing.assert_array_equal(part, ref)
+
