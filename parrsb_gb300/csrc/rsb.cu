@@ -1656,6 +1656,11 @@ struct Lanczos {
 // ----------------------------------------------------------------------------
 // RSB level helpers
 // ----------------------------------------------------------------------------
+inline bool env_flag(const char *name) {
+  const char *v = getenv(name);
+  return v && atoi(v) != 0;
+}
+
 struct HGroup {
   ll start, n;
   int p, r0;
@@ -1713,6 +1718,65 @@ __global__ void k_cc_hook(const unsigned *__restrict__ ell, const ll *__restrict
   if (i >= N) return;
   int h = half[i];
   if (h < 0) return;
+  ll sl = i >> 5;
+  const unsigned *ep = ell + slice_off[sl] + (i & 31);
+  int wd = slice_w[sl];
+  for (int k = 0; k < wd; k++) {
+    unsigned x = ep[(ll)k * 32];
+    if ((x >> 28) == 0) continue;
+    int j = x & 0x0FFFFFFF;
+    if (half[j] != h) continue;
+    int a = lab[i], b = lab[j];
+    if (a == b) continue;
+    int hi = a > b ? a : b, lo = a > b ? b : a;
+    atomicMin(&lab[hi], lo);
+    *changed = 1;
+  }
+}
+
+// Afforest-style start: hook every row to its r-th neighbour in its half
+// (one edge per row), so most of a half joins one tree before full rounds.
+__global__ void k_cc_sample(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+                            const int *__restrict__ slice_w, const int *__restrict__ half, ll N,
+                            int r, int *__restrict__ lab) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int h = half[i];
+  if (h < 0) return;
+  ll sl = i >> 5;
+  const unsigned *ep = ell + slice_off[sl] + (i & 31);
+  int wd = slice_w[sl], seen = 0;
+  for (int k = 0; k < wd; k++) {
+    unsigned x = ep[(ll)k * 32];
+    if ((x >> 28) == 0) continue;
+    int j = x & 0x0FFFFFFF;
+    if (half[j] != h) continue;
+    if (seen++ < r) continue;
+    int a = lab[i], b = lab[j];
+    if (a != b) atomicMin(&lab[a > b ? a : b], a > b ? b : a);
+    return;
+  }
+}
+
+// the root of a half's first row: presumed root of the half's largest part
+__global__ void k_cc_giant(const ll *__restrict__ hstart, int nh, const int *__restrict__ lab,
+                           int *__restrict__ giant) {
+  int h = blockIdx.x * blockDim.x + threadIdx.x;
+  if (h < nh) giant[h] = lab[hstart[h]];
+}
+
+// full round for the rows outside their half's presumed giant tree: an edge
+// between a skipped row and another row is seen from the other row (the
+// graph is symmetric), and an edge between two skipped rows joins nothing
+// new, so skipping never loses a hook
+__global__ void k_cc_hook_rest(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+                               const int *__restrict__ slice_w, const int *__restrict__ half,
+                               const int *__restrict__ giant, ll N, int *__restrict__ lab,
+                               int *__restrict__ changed) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int h = half[i];
+  if (h < 0 || lab[i] == giant[h]) return;
   ll sl = i >> 5;
   const unsigned *ep = ell + slice_off[sl] + (i & 31);
   int wd = slice_w[sl];
@@ -2125,10 +2189,34 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
       DBuf<int> lab((size_t)N), changed(1), cnt((size_t)2 * na);
       k_cc_init<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
       CK_LAUNCH();
+      // PARRSB_GPU_CC_FULL=1: every round over every row (no sampling)
+      const bool full = env_flag("PARRSB_GPU_CC_FULL");
+      const int nh = 2 * na;
+      DBuf<int> giant((size_t)nh);
+      if (!full) {
+        for (int r = 0; r < 2; r++) {
+          k_cc_sample<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
+                                                        half.p, N, r, lab.p);
+          CK_LAUNCH();
+          k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
+          CK_LAUNCH();
+        }
+        std::vector<ll> hs_by_id(nh, 0);
+        for (size_t q = 0; q < hid.size(); q++) hs_by_id[hid[q]] = hst[q];
+        DBuf<ll> hs((size_t)nh);
+        h2d(hs.p, hs_by_id.data(), nh);
+        k_cc_giant<<<grid_for(nh, 256), 256, 0, st>>>(hs.p, nh, lab.p, giant.p);
+        CK_LAUNCH();
+      }
       for (int round = 0; round < 100000; round++) {
         CK(cudaMemsetAsync(changed.p, 0, sizeof(int), st));
-        k_cc_hook<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
-                                                    half.p, N, lab.p, changed.p);
+        if (full)
+          k_cc_hook<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
+                                                      half.p, N, lab.p, changed.p);
+        else
+          k_cc_hook_rest<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p,
+                                                           lv.slice_w.p, half.p, giant.p, N,
+                                                           lab.p, changed.p);
         CK_LAUNCH();
         k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
         CK_LAUNCH();

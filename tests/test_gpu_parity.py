@@ -322,3 +322,18 @@ def test_tagged_fewer_elements_than_ranks(oracle):
     assert rc == 0
     np.testing.assert_array_equal(part, ref)
 
+
+
+@pytest.mark.parametrize("seed", [4, 5])
+def test_component_counts_sampled_equal_full_rounds(monkeypatch, seed):
+    """The sampled component count (two one-edge hooking rounds, then full
+    rounds only outside each half's presumed largest tree) counts exactly
+    what every-edge rounds count, on meshes whose halves fall apart."""
+    vtx, xyz, _ = meshgen.subboxes(12, smin=60, smax=800, delete=0.08, seed=seed)
+    a = P.part_mesh(vtx, xyz, 16, partitioner=0)
+    ca = P.last_stats().max_components
+    monkeypatch.setenv("PARRSB_GPU_CC_FULL", "1")
+    b = P.part_mesh(vtx, xyz, 16, partitioner=0)
+    cb = P.last_stats().max_components
+    np.testing.assert_array_equal(a, b)
+    assert ca == cb and ca > 1
