@@ -84,51 +84,61 @@ __global__ void k_graph_rows(const long long *__restrict__ vtx, int nv, ll N,
                              const ll *__restrict__ rowptr, int *__restrict__ col,
                              unsigned char *__restrict__ wout, ll *__restrict__ rowlen,
                              int *__restrict__ maxw) {
-  ll a = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= N) return;
-  long long va[8];
-  for (int k = 0; k < nv; k++) va[k] = vtx[a * nv + k];
-  ll cnt = 0, out = FILL ? rowptr[a] : 0;
+  const ll a = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   int wmax = 0;
-  for (int k = 0; k < nv; k++) {
-    int r = runid[inv[a * nv + k]];
-    for (ll q = run_start[r]; q < run_start[r + 1]; q++) {
-      int slot = sorted_slot[q];
-      ll b = slot / nv;
-      if (b == a) continue;
-      int l = slot - (int)b * nv;
-      long long vb[8];
-      for (int m = 0; m < nv; m++) vb[m] = vtx[b * nv + m];
-      bool first = true;
-      for (int kk = 0; kk < k && first; kk++)
-        for (int m = 0; m < nv; m++)
-          if (vb[m] == va[kk]) {
-            first = false;
-            break;
-          }
-      for (int m = 0; m < l && first; m++)
-        if (vb[m] == va[k]) first = false;
-      if (!first) continue;
-      int wt = 0;
-      for (int kk = 0; kk < nv; kk++)
-        for (int m = 0; m < nv; m++) wt += (va[kk] == vb[m]);
-      if (FILL) {
-        col[out + cnt] = (int)b;
-        wout[out + cnt] = (unsigned char)(wt > 255 ? 255 : wt);
+  if (a < N) {
+    long long va[8];
+    for (int k = 0; k < nv; k++) va[k] = vtx[a * nv + k];
+    ll cnt = 0, out = FILL ? rowptr[a] : 0;
+    for (int k = 0; k < nv; k++) {
+      int r = runid[inv[a * nv + k]];
+      for (ll q = run_start[r]; q < run_start[r + 1]; q++) {
+        int slot = sorted_slot[q];
+        ll b = slot / nv;
+        if (b == a) continue;
+        int l = slot - (int)b * nv;
+        long long vb[8];
+        for (int m = 0; m < nv; m++) vb[m] = vtx[b * nv + m];
+        bool first = true;
+        for (int kk = 0; kk < k && first; kk++)
+          for (int m = 0; m < nv; m++)
+            if (vb[m] == va[kk]) {
+              first = false;
+              break;
+            }
+        for (int m = 0; m < l && first; m++)
+          if (vb[m] == va[k]) first = false;
+        if (!first) continue;
+        int wt = 0;
+        for (int kk = 0; kk < nv; kk++)
+          for (int m = 0; m < nv; m++) wt += (va[kk] == vb[m]);
+        if (FILL) {
+          col[out + cnt] = (int)b;
+          wout[out + cnt] = (unsigned char)(wt > 255 ? 255 : wt);
+        }
+        if (wt > wmax) wmax = wt;
+        cnt++;
       }
-      if (wt > wmax) wmax = wt;
-      cnt++;
     }
+    if (!FILL) rowlen[a] = cnt;
   }
   if (!FILL) {
-    rowlen[a] = cnt;
-    atomicMax(maxw, wmax);
+    // one atomic per warp (every lane reaches this shuffle): a global atomic
+    // per row serialises on one address
+    for (int off = 16; off > 0; off >>= 1)
+      wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxw, wmax);
   }
 }
 
 __global__ void k_max_ll(const ll *__restrict__ v, ll n, unsigned long long *__restrict__ m) {
   ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) atomicMax(m, (unsigned long long)v[i]);
+  unsigned long long x = i < n ? (unsigned long long)v[i] : 0ull;
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, x, off);
+    x = y > x ? y : x;
+  }
+  if ((threadIdx.x & 31) == 0 && x) atomicMax(m, x);  // one atomic per warp
 }
 
 // ----------------------------------------------------------------------------
