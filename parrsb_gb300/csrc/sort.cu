@@ -9,7 +9,9 @@
 // Per pass: a tile histogram kernel (4096 items per 256-thread CTA), a
 // per-digit exclusive scan over tiles, and a scatter kernel that ranks items
 // stably inside the CTA with __match_any_sync (warp w owns items
-// [w*512, w*512+512) of the tile, processed 32 at a time in order).  One
+// [w*512, w*512+512) of the tile, processed 32 at a time in order), stages
+// the tile in shared memory in digit order and writes each digit's run with
+// consecutive addresses.  One
 // up-front kernel builds the global digit histograms of every pass; passes
 // whose digit is constant over all items are skipped.
 #include "sort.cuh"
@@ -22,6 +24,7 @@ constexpr int SORT_THREADS = 256;
 constexpr int ITEMS_PER_THREAD = 16;
 constexpr int TILE = SORT_THREADS * ITEMS_PER_THREAD;  // 4096
 constexpr int MAX_PASSES = 12;                           // 8 key + 4 seg bytes
+constexpr size_t SCATTER_SMEM = (size_t)TILE * (8 + 4 + 1);  // staged keys, values, digits
 
 struct PassDesc {
   int is_seg;
@@ -135,6 +138,11 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
   constexpr int NW = SORT_THREADS / 32;
   __shared__ u32 wcnt[NW][256];
   __shared__ u32 dbase[256];
+  __shared__ u32 tl[256];  // tile-local start of each digit
+  extern __shared__ __align__(16) unsigned char sc_smem[];
+  u64 *skey = reinterpret_cast<u64 *>(sc_smem);             // TILE
+  int *sval = reinterpret_cast<int *>(skey + TILE);          // TILE
+  unsigned char *sdig = reinterpret_cast<unsigned char *>(sval + TILE);  // TILE
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
   // exclusive scan of the 256 digit totals (one value per thread)
@@ -182,7 +190,7 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
     __syncwarp();
   }
   __syncthreads();
-  // exclusive scan over warps per digit
+  // exclusive scan over warps per digit, then over the digits of the tile
   {
     int d = threadIdx.x;
     u32 run = 0;
@@ -192,15 +200,39 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
       wcnt[w][d] = run;
       run += t;
     }
+    u32 x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      u32 y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __shared__ u32 ws2[NW];
+    if (lane == 31) ws2[warp] = x;
+    __syncthreads();
+    u32 off = 0;
+    for (int w = 0; w < warp; w++) off += ws2[w];
+    tl[d] = off + x - run;
   }
   __syncthreads();
+  // stage the tile in digit order, then write every digit run with
+  // consecutive addresses (coalesced stores instead of 256 scattered streams)
 #pragma unroll
   for (int r = 0; r < ITEMS_PER_THREAD; r++) {
     if (dig[r] < 256) {
-      u32 pos = dbase[dig[r]] + wcnt[warp][dig[r]] + rank[r];
-      kout[pos] = key[r];
-      vout[pos] = val[r];
+      const u32 lp = tl[dig[r]] + wcnt[warp][dig[r]] + rank[r];
+      skey[lp] = key[r];
+      sval[lp] = val[r];
+      sdig[lp] = (unsigned char)dig[r];
     }
+  }
+  __syncthreads();
+  const ll t0 = (ll)blockIdx.x * TILE;
+  const int tn = (int)(n - t0 < TILE ? n - t0 : TILE);
+  for (int t = threadIdx.x; t < tn; t += blockDim.x) {
+    const u32 d = sdig[t];
+    const u32 pos = dbase[d] + ((u32)t - tl[d]);
+    kout[pos] = skey[t];
+    vout[pos] = sval[t];
   }
 }
 
@@ -246,6 +278,12 @@ void seg_sort_pairs(DBuf<u64> &keys, DBuf<int> &vals, ll n,
     passes[npasses].shift = b >= nkey ? 8 * (b - nkey) : 8 * b;
     npasses++;
   }
+  static bool scatter_attr = false;  // staging buffers exceed the 48 KB default
+  if (!scatter_attr) {
+    CK(cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)SCATTER_SMEM));
+    scatter_attr = true;
+  }
   for (int q = 0; q < npasses; q++) {
     const PassDesc &pd = passes[q];
     k_tile_hist<<<ntiles, SORT_THREADS, 0, st>>>(keys.p, vals.p, n, seg_of_val,
@@ -254,7 +292,7 @@ void seg_sort_pairs(DBuf<u64> &keys, DBuf<int> &vals, ll n,
     CK_LAUNCH();
     k_tile_scan<<<256, 1024, 0, st>>>(ws.counts.p, ntiles, ws.totals.p);
     CK_LAUNCH();
-    k_scatter<<<ntiles, SORT_THREADS, 0, st>>>(keys.p, vals.p, ws.ktmp.p,
+    k_scatter<<<ntiles, SORT_THREADS, SCATTER_SMEM, st>>>(keys.p, vals.p, ws.ktmp.p,
                                                ws.vtmp.p, n, seg_of_val,
                                                pd.is_seg, pd.shift, ws.counts.p,
                                                ws.totals.p, ntiles);
