@@ -413,13 +413,15 @@ __global__ void k_rank_write(const u64 *__restrict__ keys, const int *__restrict
 //             is the number of elements of its sub-range before it in
 //             (rank, position) order; otherwise an LSD radix in shared memory
 //             over the varying bytes of the rank, then of the sub-range start
-//             (warp w ranks positions [512 w, 512 w + 512) in order with
+//             (warp w ranks positions [SMALL_SPAN w, SMALL_SPAN (w + 1)) in order with
 //             __match_any_sync).
 // Gives exactly the order of the level-by-level global path.
 // ---------------------------------------------------------------------------
 constexpr int SMALL_MAX = 8192;
-constexpr int SMALL_THREADS = 512;
-constexpr int SMALL_ITEMS = 16;   // SMALL_MAX / SMALL_THREADS
+constexpr int SMALL_THREADS = 1024;
+constexpr int SMALL_WARPS = SMALL_THREADS / 32;
+constexpr int SMALL_ITEMS = SMALL_MAX / SMALL_THREADS;  // positions per thread
+constexpr int SMALL_SPAN = 32 * SMALL_ITEMS;            // positions per warp
 constexpr int SMALL_CMP = 256;    // comparison ranking up to this sub-range length
 constexpr int SMALL_SHORT = 32;   // sequential boxes up to this sub-range length
 constexpr int SMALL_NLONG = SMALL_MAX / SMALL_SHORT;  // box table slots
@@ -472,7 +474,7 @@ __device__ __forceinline__ u32 kx_key(const u32 *rk, const unsigned char *sax, u
 // shared memory of k_rcb_small
 constexpr size_t small_smem_bytes() {
   return (size_t)SMALL_MAX * (3 * 4 /*rk*/ + 4 + 4 /*item, item2*/ + 4 /*kx*/ + 1 /*sax*/) +
-         (size_t)16 * 256 * 2 /*wcnt*/ + (size_t)SMALL_NLONG * 6 * 4 /*box*/;
+         (size_t)SMALL_WARPS * 256 * 2 /*wcnt*/ + (size_t)SMALL_NLONG * 6 * 4 /*box*/;
 }
 
 template <bool LOCAL>
@@ -488,8 +490,8 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
   u32 *item2 = item + SMALL_MAX;
   u32 *kx = item2 + SMALL_MAX;         // axis rank per position
   u32 *box = kx + SMALL_MAX;           // [SMALL_NLONG][6] min0..2, max0..2
-  unsigned short *wcnt = (unsigned short *)(box + SMALL_NLONG * 6);  // [16][256]
-  unsigned char *sax = (unsigned char *)(wcnt + 16 * 256);  // axis by sub-range start
+  unsigned short *wcnt = (unsigned short *)(box + SMALL_NLONG * 6);  // [SMALL_WARPS][256]
+  unsigned char *sax = (unsigned char *)(wcnt + SMALL_WARPS * 256);  // axis by sub-range start
   __shared__ unsigned dbase[256];
   __shared__ u32 s_and, s_or, s_stand, s_stor;
   __shared__ int s_maxlen;
@@ -521,7 +523,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
-      int x = warp * 512 + r * 32 + lane;
+      int x = warp * SMALL_SPAN + r * 32 + lane;
       st_r[r] = -1, len_r[r] = 0;
       if (x < n) {
         SubR sr = descend<LOCAL>(x, n, p0, d);
@@ -535,7 +537,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
     // ---- bounding boxes on dense ranks, axis of each sub-range
 #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
-      const int x = warp * 512 + r * 32 + lane;
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
       const int st = st_r[r], len = len_r[r];
       if (len > 0 && len <= SMALL_SHORT && st == x) {  // short: sequential
         u32 mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
@@ -592,7 +594,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
     if (maxlen > SMALL_SHORT) {
 #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = warp * 512 + r * 32 + lane;
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
         if (len_r[r] > SMALL_SHORT && st_r[r] == x) {
           const int o = x / SMALL_SHORT;
           double best = 0.0;
@@ -611,7 +613,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
     u32 kand = 0xFFFFFFFFu, kor = 0u, stand = 0xFFFFFFFFu, stor = 0u;
 #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
-      const int x = warp * 512 + r * 32 + lane;
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
       if (x >= n) continue;
       const u32 st = (u32)st_r[r];
       const u32 id = item[x] & 0xFFFFu;
@@ -625,7 +627,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
       // ---- comparison ranking inside each sub-range
 #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = warp * 512 + r * 32 + lane;
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
         if (x >= n) continue;
         const int len = len_r[r], st = st_r[r];
         if (!len) {
@@ -658,13 +660,13 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
         const bool is_st = b >= 4;
         const int shift = is_st ? 8 * (b - 4) : 8 * b;
         if ((((is_st ? sdiff : kdiff) >> shift) & 255u) == 0) continue;
-        for (int i = threadIdx.x; i < 16 * 256; i += blockDim.x) wcnt[i] = 0;
+        for (int i = threadIdx.x; i < SMALL_WARPS * 256; i += blockDim.x) wcnt[i] = 0;
         __syncthreads();
         unsigned rkk[SMALL_ITEMS], dg[SMALL_ITEMS];
         u32 itv[SMALL_ITEMS];
 #pragma unroll
         for (int r = 0; r < SMALL_ITEMS; r++) {
-          const int x = warp * 512 + r * 32 + lane;
+          const int x = warp * SMALL_SPAN + r * 32 + lane;
           unsigned dgt = 256;
           itv[r] = 0;
           if (x < n) {
@@ -689,7 +691,7 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
         __syncthreads();
         if (threadIdx.x < 256) {
           unsigned run = 0;
-          for (int w = 0; w < 16; w++) {
+          for (int w = 0; w < SMALL_WARPS; w++) {
             unsigned t = wcnt[w * 256 + threadIdx.x];
             wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
             run += t;
@@ -724,13 +726,13 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
   int ev[SMALL_ITEMS];
 #pragma unroll
   for (int r = 0; r < SMALL_ITEMS; r++) {
-    const int x = warp * 512 + r * 32 + lane;
+    const int x = warp * SMALL_SPAN + r * 32 + lane;
     ev[r] = x < n ? perm[start + (item[x] & 0xFFFFu)] : 0;
   }
   __syncthreads();
 #pragma unroll
   for (int r = 0; r < SMALL_ITEMS; r++) {
-    const int x = warp * 512 + r * 32 + lane;
+    const int x = warp * SMALL_SPAN + r * 32 + lane;
     if (x < n) {
       perm[start + x] = ev[r];
       if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
