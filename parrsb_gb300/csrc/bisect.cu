@@ -834,6 +834,14 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
   DBuf<int> nact_d(1);
   DBuf<unsigned long long> maxn_d(1);
   const size_t small_smem = small_smem_bytes();
+  // PARRSB_GPU_LEVEL_LOG=1: per-level times on stderr (synchronises)
+  const bool level_log = getenv("PARRSB_GPU_LEVEL_LOG") != nullptr;
+  cudaEvent_t lg_e0 = nullptr, lg_e1 = nullptr;
+  if (level_log) {
+    CK(cudaEventCreate(&lg_e0));
+    CK(cudaEventCreate(&lg_e1));
+    CK(cudaEventRecord(lg_e0, st));
+  }
   if (kind == BISECT_RCB && ws.rank_of != cent) {
     // dense ranks of the centroid coordinates, once per set of centroids
     ws.rank.ensure((size_t)3 * N);
@@ -870,6 +878,15 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
     d2h(&nact, nact_d.p, 1);
     d2h(&maxn, maxn_d.p, 1);
     sync();
+    if (level_log && kind == BISECT_RCB) {  // time of the global levels so far
+      CK(cudaEventRecord(lg_e1, st));
+      CK(cudaEventSynchronize(lg_e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, lg_e0, lg_e1));
+      fprintf(stderr, "parrsb_gb300: rcb level %d segments=%lld active=%d max_n=%llu: %.3f ms\n",
+              level, (long long)nseg, nact, maxn, ms);
+      CK(cudaEventRecord(lg_e0, st));
+    }
     if (kind == BISECT_RCB && nact > 0 && maxn <= (unsigned long long)SMALL_MAX) {
       // every remaining level of every segment in one launch
       if (do_local) {
@@ -886,6 +903,16 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
             part_of_elem);
       }
       CK_LAUNCH();
+      if (level_log) {
+        CK(cudaEventRecord(lg_e1, st));
+        CK(cudaEventSynchronize(lg_e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, lg_e0, lg_e1));
+        fprintf(stderr, "parrsb_gb300: rcb small-segment kernel segments=%lld: %.3f ms\n",
+                (long long)nseg, ms);
+        cudaEventDestroy(lg_e0);
+        cudaEventDestroy(lg_e1);
+      }
       return;
     }
     fill_seg_of_pos(t, ws.seg_of_pos.p, N);

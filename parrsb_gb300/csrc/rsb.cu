@@ -1592,6 +1592,10 @@ struct Lanczos {
     }
     const long long per_pass_kernels = 4 + (long long)MI * 3 + 5;
     launches = 0;
+    // PARRSB_GPU_LEVEL_LOG=1 (timing mode): one line per level on stderr
+    const bool level_log = !ev.empty() && getenv("PARRSB_GPU_LEVEL_LOG");
+    const double spmv0 = ctx().stats.spmv_ms, pass0 = ctx().stats.lanczos_ms[5];
+    int npass = 0;
     for (int pass = 0; pass < mpass; pass++) {
       CK(cudaMemsetAsync(any.p, 0, 2 * sizeof(int), st));
       if (use_graph) {
@@ -1606,6 +1610,7 @@ struct Lanczos {
       sync();
       launches += h_any[1];  // SpMV launches that did work this pass
       ctx().stats.lanczos_passes++;
+      npass++;
       if (!ev.empty()) {
         auto el = [&](cudaEvent_t a, cudaEvent_t b) {
           float ms = 0.f;
@@ -1626,6 +1631,13 @@ struct Lanczos {
       }
       if (!h_any[0]) break;
     }
+    if (level_log)
+      fprintf(stderr,
+              "parrsb_gb300: level rows=%lld groups=%d tiles=%d passes=%d steps=%lld "
+              "spmv_ms=%.2f (%.4f per step) pass_ms=%.2f\n",
+              (long long)N, A, T, npass, launches, ctx().stats.spmv_ms - spmv0,
+              launches ? (ctx().stats.spmv_ms - spmv0) / launches : 0.0,
+              ctx().stats.lanczos_ms[5] - pass0);
     for (auto &e : ev) cudaEventDestroy(e);
     ev.clear();
     for (auto &e : evk) cudaEventDestroy(e);
