@@ -644,7 +644,7 @@ __device__ __forceinline__ double LaneSum<double>::chunk() const { return warp_t
 // one chunk per warp on smaller ones so that enough warps fill the GPU
 constexpr ll PR_BIG = 1ll << 22;
 
-template <typename VT, int MODE, int PR_U>
+template <typename VT, int MODE, int PR_U, bool FUSE = true>
 __global__ void __launch_bounds__(512)
 k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
      GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
@@ -704,7 +704,7 @@ k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__rest
     double v0 = tile_total(cs, nc);
     if (threadIdx.x == 0) part[t] = v0;
   }
-  fused_fin<OP>(gs, g, part, fa, sh);
+  if (FUSE) fused_fin<OP>(gs, g, part, fa, sh);
 }
 
 // threads per block of k_pr / k_ritz for tiles of at most `rows` rows
@@ -1338,6 +1338,13 @@ struct Lanczos {
   DBuf<int> err;                 // [0]: a staged-SpMV wait gave up
   int pr_bd = 256;               // threads per block of k_pr
   int pr_u = 4;                  // chunks per warp in flight in k_pr
+  // The vector updates write tile partials and a separate one-block-per-group
+  // launch finalises (measured faster than finalising in the last tile block
+  // of each group, which every block pays for with a fence, an atomic and
+  // barriers); PARRSB_GPU_PR_FUSED=1 selects the fused form (same bits).
+  bool pr_fused = false;
+  // the same choice for the SpMV (PARRSB_GPU_SPMV_FUSED=1: fused)
+  bool sp_fused = false;
   int ritz_bd = 256;             // threads per block of k_ritz
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
 
@@ -1369,6 +1376,12 @@ struct Lanczos {
     ll max_tile = 0;
     for (int g = 0; g < A; g++) max_tile = std::max(max_tile, std::min(tile_rows(gn[g]), gn[g]));
     pr_u = N >= PR_BIG ? 4 : 1;
+    {
+      const char *v = getenv("PARRSB_GPU_PR_FUSED");
+      pr_fused = v && atoi(v) != 0;
+      const char *v2 = getenv("PARRSB_GPU_SPMV_FUSED");
+      sp_fused = v2 && atoi(v2) != 0;
+    }
     pr_bd = vec_threads<VT>(max_tile, pr_u);
     ritz_bd = vec_threads<VT>(max_tile, 1);
     VS = (N + 63) & ~(ll)63;
@@ -1453,18 +1466,33 @@ struct Lanczos {
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
       mark(4 * it + 0);
-      (pr_u == 4 ? k_pr<VT, TM_P, 4> : k_pr<VT, TM_P, 1>)<<<T, pr_bd, 0, st>>>(
-          tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-      CK_LAUNCH();
+      if (pr_fused) {
+        (pr_u == 4 ? k_pr<VT, TM_P, 4> : k_pr<VT, TM_P, 1>)<<<T, pr_bd, 0, st>>>(
+            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
+        CK_LAUNCH();
+      } else {  // tile partials, then one block per group
+        (pr_u == 4 ? k_pr<VT, TM_P, 4, false> : k_pr<VT, TM_P, 1, false>)<<<T, pr_bd, 0, st>>>(
+            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
+        CK_LAUNCH();
+        fin<FIN_PMEAN, GATE_RUN>(it, tol, mpass);
+      }
       mark(4 * it + 1);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
-      spmv(lv, sp_kind, bd, fargs(it, tol, mpass), 1, 0);
+      spmv(lv, sp_kind, bd, fargs(it, tol, mpass), sp_fused ? 1 : 0, 0);
+      if (!sp_fused) fin<FIN_PAP, GATE_RUN>(it, tol, mpass);
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       mark(4 * it + 2);
-      (pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>)<<<T, pr_bd, 0, st>>>(
-          tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-      CK_LAUNCH();
+      if (pr_fused) {
+        (pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>)<<<T, pr_bd, 0, st>>>(
+            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
+        CK_LAUNCH();
+      } else {
+        (pr_u == 4 ? k_pr<VT, TM_R, 4, false> : k_pr<VT, TM_R, 1, false>)<<<T, pr_bd, 0, st>>>(
+            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
+        CK_LAUNCH();
+        fin<FIN_RTR, GATE_RUN>(it, tol, mpass);
+      }
       mark(4 * it + 3);
     }
     mark(4 * MI + 2);

@@ -337,3 +337,17 @@ def test_component_counts_sampled_equal_full_rounds(monkeypatch, seed):
     cb = P.last_stats().max_components
     np.testing.assert_array_equal(a, b)
     assert ca == cb and ca > 1
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+def test_rsb_fused_finalisation_same_bits(monkeypatch, fp32):
+    """Finalising a group's scalars in the last tile block (fused) or in a
+    separate one-block-per-group launch reduces the same partials in the same
+    order: bitwise the same partition."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", fp32)
+    vtx, xyz = meshgen.box_hex(20, 16, 12, jitter=0.1, seed=16)
+    a = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    monkeypatch.setenv("PARRSB_GPU_PR_FUSED", "1")
+    monkeypatch.setenv("PARRSB_GPU_SPMV_FUSED", "1")
+    b = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    np.testing.assert_array_equal(a, b)
