@@ -460,10 +460,10 @@ def main():
         "stage_ms": dict(zip(P.STAGES, [round(x, 2) for x in s.stage_ms])),
         "lanczos_breakdown_ms": dict(zip(["p_update", "r_update", "eigensolve", "ritz",
                                           "pass_setup", "pass_device_total"],
-                                         [round(x / args.steps, 2) for x in
+                                         [round(x / len(stats), 2) for x in
                                           [sum(st.lanczos_ms[i] for st in stats)
                                            for i in range(6)]])),
-        "lanczos_spmv_ms": round(spmv_ms / args.steps, 2),
+        "lanczos_spmv_ms": round(spmv_ms / len(stats), 2),
         "lanczos_passes": int(s.lanczos_passes),
     }
     if rank == 0:
