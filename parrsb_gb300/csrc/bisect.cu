@@ -36,41 +36,11 @@ __global__ void k_centroids(const double *__restrict__ xyz, int nel, int nv,
   cent[2 * (ll)nel + e] = c[2];
 }
 
-enum Gen { GEN_BBOX = 0, GEN_MEAN = 1, GEN_INERTIA = 2, GEN_ARRAY = 3 };
+enum Gen { GEN_MEAN = 1, GEN_INERTIA = 2, GEN_ARRAY = 3 };
 
 // Segment "active" rule shared by all kernels.
 __device__ __forceinline__ bool seg_active(int p, ll n, int do_local) {
   return p > 1 || (do_local && p == 1 && n >= 2);
-}
-
-// Bounding boxes are reduced on order-preserving integer keys (integer
-// min / max instead of the low-throughput FP64 pipe); the key's bits travel
-// in the double arrays of the tree.
-__device__ __forceinline__ double key_bits(double x) {
-  return __longlong_as_double((long long)ordered_key(x));
-}
-__device__ __forceinline__ double bits_to_value(double kb) {
-  unsigned long long k = (unsigned long long)__double_as_longlong(kb);
-  unsigned long long b = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
-  return __longlong_as_double((long long)b);
-}
-__device__ __forceinline__ double warp_min_key(double v) {
-  unsigned long long k = (unsigned long long)__double_as_longlong(v);
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_down_sync(0xffffffffu, k, off);
-    k = o < k ? o : k;
-  }
-  return __longlong_as_double((long long)k);
-}
-__device__ __forceinline__ double warp_max_key(double v) {
-  unsigned long long k = (unsigned long long)__double_as_longlong(v);
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_down_sync(0xffffffffu, k, off);
-    k = o > k ? o : k;
-  }
-  return __longlong_as_double((long long)k);
 }
 
 __device__ __forceinline__ ll find_seg(const ll *off, ll nseg, ll w) {
@@ -87,8 +57,8 @@ __device__ __forceinline__ ll find_seg(const ll *off, ll nseg, ll w) {
 
 // One warp per 32-item tile of a segment.  Level 0 generates values from
 // elements; later levels reduce the previous level's tile values.
-// For GEN_BBOX values 0..2 are minima, 3..5 maxima; otherwise sums.
-template <int V, int GEN, bool BBOX>
+// Values are sums (canonical shuffle tree).
+template <int V, int GEN>
 __global__ void k_seg_tree(const int *__restrict__ perm,
                            const double *__restrict__ cent, ll N,
                            const ll *__restrict__ seg_start,
@@ -108,12 +78,7 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
   bool valid = i < m;
   double v[V];
 #pragma unroll
-  for (int q = 0; q < V; q++) {
-    if (BBOX)  // identities of min / max on ordered keys
-      v[q] = __longlong_as_double(q < 3 ? (long long)~0ull : 0ll);
-    else
-      v[q] = 0.0;
-  }
+  for (int q = 0; q < V; q++) v[q] = 0.0;
   if (valid) {
     if (GEN == GEN_ARRAY) {
       ll src = (in_off[s] + i) * V;
@@ -122,10 +87,7 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
     } else {
       int e = perm[seg_start[s] + i];
       double c0 = cent[e], c1 = cent[N + e], c2 = cent[2 * N + e];
-      if (GEN == GEN_BBOX) {
-        v[0] = key_bits(c0), v[1] = key_bits(c1), v[2] = key_bits(c2);
-        v[3] = v[0], v[4] = v[1], v[5] = v[2];
-      } else if (GEN == GEN_MEAN) {
+      if (GEN == GEN_MEAN) {
         v[0] = c0, v[1] = c1;
         if (V > 2) v[V - 1] = c2;
       } else {  // inertia products (00, 01, 02, 11, 12, 22)
@@ -151,8 +113,6 @@ __global__ void k_seg_tree(const int *__restrict__ perm,
     double r;
     if (copy_only)
       r = v[q];
-    else if (BBOX)
-      r = q < 3 ? warp_min_key(v[q]) : warp_max_key(v[q]);
     else
       r = warp_tree_sum(v[q]);
     if (lane == 0) out[w * V + q] = r;
@@ -165,15 +125,108 @@ __global__ void k_tile_counts(const ll *__restrict__ cnt, ll nseg,
   if (s < nseg) tiles[s] = (cnt[s] + 31) / 32;
 }
 
-__global__ void k_rcb_axis(const double *__restrict__ bbox, const int *__restrict__ p,
-                           const ll *__restrict__ n, ll nseg, int ndim,
-                           int do_local, int *__restrict__ axis) {
+// RCB boxes on the dense coordinate ranks: per segment and axis the minimum
+// rank (slots 0..2) and the minimum complemented rank (slots 3..5, i.e. the
+// maximum).  Integer atomics are order-independent, so the box does not
+// depend on the grid; uniq[rank] turns a rank back into the exact coordinate.
+// A thread reduces RBOX_ITEMS consecutive positions, a warp and then the
+// block combine when they cover one segment (the common case), and only the
+// threads that straddle a segment boundary issue their own atomics.
+constexpr int RBOX_THREADS = 256, RBOX_ITEMS = 16;
+
+__device__ __forceinline__ void rbox_flush(u32 *rbox, int s, int ndim, const u32 *v) {
+  for (int a = 0; a < ndim; a++) {
+    atomicMin(&rbox[6 * (ll)s + a], v[a]);
+    atomicMin(&rbox[6 * (ll)s + 3 + a], v[3 + a]);
+  }
+}
+
+__global__ void __launch_bounds__(RBOX_THREADS)
+k_rank_box(const int *__restrict__ perm, const u32 *__restrict__ rank, ll N, int ndim,
+           const int *__restrict__ seg_of_pos, u32 *__restrict__ rbox) {
+  constexpr int NWB = RBOX_THREADS / 32;
+  __shared__ int wseg[NWB];
+  __shared__ u32 wval[NWB][6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const ll i0 = ((ll)blockIdx.x * RBOX_THREADS + threadIdx.x) * RBOX_ITEMS;
+  int sg[RBOX_ITEMS], el[RBOX_ITEMS];
+#pragma unroll
+  for (int r = 0; r < RBOX_ITEMS; r++) {
+    const bool ok = i0 + r < N;
+    sg[r] = ok ? seg_of_pos[i0 + r] : -1;
+    el[r] = ok ? perm[i0 + r] : 0;
+  }
+  u32 rk[3][RBOX_ITEMS];
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int r = 0; r < RBOX_ITEMS; r++)
+      rk[a][r] = (a < ndim && sg[r] >= 0) ? rank[(ll)a * N + el[r]] : 0u;
+  int s = -1;
+  u32 v[6];
+#pragma unroll
+  for (int q = 0; q < 6; q++) v[q] = ~0u;
+#pragma unroll
+  for (int r = 0; r < RBOX_ITEMS; r++) {
+    if (sg[r] < 0) continue;
+    if (sg[r] != s) {  // a segment boundary inside this thread's run
+      if (s >= 0) rbox_flush(rbox, s, ndim, v);
+#pragma unroll
+      for (int q = 0; q < 6; q++) v[q] = ~0u;
+      s = sg[r];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      v[a] = min(v[a], rk[a][r]);
+      v[3 + a] = min(v[3 + a], ~rk[a][r]);
+    }
+  }
+  // warp: one segment among the lanes that hold one -> shuffle-free reduce
+  const int smin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(s >= 0 ? s : 0x7fffffff));
+  const int smax = (int)__reduce_max_sync(0xffffffffu, (unsigned)(s + 1)) - 1;
+  if (smax >= 0 && smin == smax) {
+#pragma unroll
+    for (int q = 0; q < 6; q++) v[q] = __reduce_min_sync(0xffffffffu, v[q]);
+    if (lane == 0) {
+      wseg[warp] = smax;
+#pragma unroll
+      for (int q = 0; q < 6; q++) wval[warp][q] = v[q];
+    }
+  } else {
+    if (s >= 0) rbox_flush(rbox, s, ndim, v);
+    if (lane == 0) wseg[warp] = -1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int ws = lane < NWB ? wseg[lane] : -1;
+    const int bmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(ws >= 0 ? ws : 0x7fffffff));
+    const int bmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)(ws + 1)) - 1;
+    u32 bv[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) bv[q] = ws >= 0 ? wval[lane < NWB ? lane : 0][q] : ~0u;
+    if (bmax >= 0 && bmin == bmax) {
+#pragma unroll
+      for (int q = 0; q < 6; q++) bv[q] = __reduce_min_sync(0xffffffffu, bv[q]);
+      if (lane == 0) rbox_flush(rbox, bmax, ndim, bv);
+    } else if (ws >= 0) {
+      rbox_flush(rbox, ws, ndim, bv);
+    }
+  }
+}
+
+// Longest box edge per segment from the rank boxes (strictly longer wins, so
+// ties keep the lower axis, as with coordinate boxes).
+__global__ void k_rcb_axis_rank(const u32 *__restrict__ rbox, const double *__restrict__ uniq,
+                                ll N, const int *__restrict__ p, const ll *__restrict__ n,
+                                ll nseg, int ndim, int do_local, int *__restrict__ axis) {
   ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
-  const double *b = bbox + 6 * s;
-  double len[3];
-  for (int d = 0; d < ndim; d++)
-    len[d] = __dsub_rn(bits_to_value(b[3 + d]), bits_to_value(b[d]));
+  double len[3] = {0.0, 0.0, 0.0};
+  if (n[s] > 0)
+    for (int d = 0; d < ndim; d++) {
+      const u32 lo = rbox[6 * s + d], hi = ~rbox[6 * s + 3 + d];
+      len[d] = __dsub_rn(uniq[(ll)d * N + hi], uniq[(ll)d * N + lo]);
+    }
   int ax = 0;
   for (int d = 1; d < ndim; d++)
     if (len[d] > len[ax]) ax = d;
@@ -297,9 +350,10 @@ __global__ void k_keys(const int *__restrict__ perm, const double *__restrict__ 
   int s = seg_of_pos[i];
   int e = perm[i];
   u64 k = 0;
-  if (KIND == BISECT_RCB) {  // dense rank (order-equivalent to the coordinate)
+  if (KIND == BISECT_RCB) {  // segment id above the dense rank of the coordinate
     int ax = axis_or_act[s];
-    if (ax >= 0) k = rank[(ll)ax * N + e];
+    k = (u64)(unsigned)s << 32;
+    if (ax >= 0) k |= rank[(ll)ax * N + e];
   } else {
     if (axis_or_act[s]) {
       const double *a = avg + 3 * s, *v = ev + 3 * s;
@@ -312,7 +366,7 @@ __global__ void k_keys(const int *__restrict__ perm, const double *__restrict__ 
   }
   keys[i] = k;
   vals[i] = e;
-  seg_of_elem[e] = s;
+  if (KIND != BISECT_RCB) seg_of_elem[e] = s;
 }
 
 __global__ void k_child_counts(const int *__restrict__ p, const ll *__restrict__ n,
@@ -748,7 +802,7 @@ __global__ void k_max_active_n(const int *__restrict__ p, const ll *__restrict__
 
 // Run the tile tree over every segment of `t` until one value per segment
 // is left; result in out_final (nseg * V values).
-template <int V, int GEN0, bool BBOX>
+template <int V, int GEN0>
 void seg_tree_reduce(const int *perm, const double *cent, ll N, SegTable &t,
                      const double *avg, BisectWs &ws, double *out_final) {
   cudaStream_t st = ctx().stream;
@@ -768,11 +822,11 @@ void seg_tree_reduce(const int *perm, const double *cent, ll N, SegTable &t,
     ob.ensure((size_t)ntiles * V);
     unsigned blocks = grid_for(ntiles * 32, 256);
     if (first)
-      k_seg_tree<V, GEN0, BBOX><<<blocks, 256, 0, st>>>(perm, cent, N, t.start.p,
+      k_seg_tree<V, GEN0><<<blocks, 256, 0, st>>>(perm, cent, N, t.start.p,
                                                         cnt.p, nseg, off.p, ntiles,
                                                         nullptr, nullptr, avg, ob.p);
     else
-      k_seg_tree<V, GEN_ARRAY, BBOX><<<blocks, 256, 0, st>>>(
+      k_seg_tree<V, GEN_ARRAY><<<blocks, 256, 0, st>>>(
           perm, cent, N, t.start.p, cnt.p, nseg, off.p, ntiles, in, in_off.p, avg,
           ob.p);
     CK_LAUNCH();
@@ -836,12 +890,17 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
   const size_t small_smem = small_smem_bytes();
   // PARRSB_GPU_LEVEL_LOG=1: per-level times on stderr (synchronises)
   const bool level_log = getenv("PARRSB_GPU_LEVEL_LOG") != nullptr;
-  cudaEvent_t lg_e0 = nullptr, lg_e1 = nullptr;
+  cudaEvent_t lg_e0 = nullptr, lg_e1 = nullptr, lg_part[4] = {};
+  float lg_sum[4] = {};  // box + axis, keys, sort, children: summed over levels
   if (level_log) {
     CK(cudaEventCreate(&lg_e0));
     CK(cudaEventCreate(&lg_e1));
+    for (auto &e : lg_part) CK(cudaEventCreate(&e));
     CK(cudaEventRecord(lg_e0, st));
   }
+  auto lg_mark = [&](int i) {
+    if (level_log && kind == BISECT_RCB) CK(cudaEventRecord(lg_part[i], st));
+  };
   if (kind == BISECT_RCB && ws.rank_of != cent) {
     // dense ranks of the centroid coordinates, once per set of centroids
     ws.rank.ensure((size_t)3 * N);
@@ -883,8 +942,15 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
       CK(cudaEventSynchronize(lg_e1));
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, lg_e0, lg_e1));
-      fprintf(stderr, "parrsb_gb300: rcb level %d segments=%lld active=%d max_n=%llu: %.3f ms\n",
-              level, (long long)nseg, nact, maxn, ms);
+      if (level > 0) {
+        float d[4];
+        CK(cudaEventElapsedTime(&d[0], lg_e0, lg_part[0]));
+        for (int i = 1; i < 4; i++) CK(cudaEventElapsedTime(&d[i], lg_part[i - 1], lg_part[i]));
+        for (int i = 0; i < 4; i++) lg_sum[i] += d[i];
+      }
+      fprintf(stderr, "parrsb_gb300: rcb level %d segments=%lld active=%d max_n=%llu: %.3f ms"
+              " (sums box %.2f keys %.2f sort %.2f children %.2f)\n",
+              level, (long long)nseg, nact, maxn, ms, lg_sum[0], lg_sum[1], lg_sum[2], lg_sum[3]);
       CK(cudaEventRecord(lg_e0, st));
     }
     if (kind == BISECT_RCB && nact > 0 && maxn <= (unsigned long long)SMALL_MAX) {
@@ -912,27 +978,35 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
                 (long long)nseg, ms);
         cudaEventDestroy(lg_e0);
         cudaEventDestroy(lg_e1);
+        for (auto &e : lg_part) cudaEventDestroy(e);
       }
       return;
     }
+    if (level_log && kind == BISECT_RCB) CK(cudaEventRecord(lg_e0, st));
     fill_seg_of_pos(t, ws.seg_of_pos.p, N);
     if (nact == 0) break;
     ws.axis.ensure((size_t)nseg);
     if (kind == BISECT_RCB) {
-      DBuf<double> bbox((size_t)nseg * 6);
-      seg_tree_reduce<6, GEN_BBOX, true>(perm.p, cent, N, t, nullptr, ws, bbox.p);
-      k_rcb_axis<<<grid_for(nseg, 256), 256, 0, st>>>(bbox.p, t.p.p, t.n.p, nseg, ndim,
-                                                      do_local, ws.axis.p);
+      ws.rbox.ensure((size_t)nseg * 6);
+      CK(cudaMemsetAsync(ws.rbox.p, 0xFF, (size_t)nseg * 6 * sizeof(u32), st));
+      k_rank_box<<<grid_for(N, RBOX_THREADS * RBOX_ITEMS), RBOX_THREADS, 0, st>>>(
+          perm.p, ws.rank.p, N, ndim, ws.seg_of_pos.p, ws.rbox.p);
       CK_LAUNCH();
+      k_rcb_axis_rank<<<grid_for(nseg, 256), 256, 0, st>>>(ws.rbox.p, ws.uniq.p, N, t.p.p,
+                                                           t.n.p, nseg, ndim, do_local,
+                                                           ws.axis.p);
+      CK_LAUNCH();
+      lg_mark(0);
       k_keys<BISECT_RCB><<<grid_for(N, 256), 256, 0, st>>>(
           perm.p, cent, ws.rank.p, N, ws.seg_of_pos.p, ws.axis.p, nullptr, nullptr, ws.keys.p,
           ws.vals.p, ws.seg_of_elem.p);
       CK_LAUNCH();
+      lg_mark(1);
     } else {
       DBuf<double> sums((size_t)nseg * 3), avg((size_t)nseg * 3),
           isums((size_t)nseg * 6);
       ws.ev.ensure((size_t)nseg * 3);
-      seg_tree_reduce<3, GEN_MEAN, false>(perm.p, cent, N, t, nullptr, ws, sums.p);
+      seg_tree_reduce<3, GEN_MEAN>(perm.p, cent, N, t, nullptr, ws, sums.p);
       k_rib_mean_group<<<grid_for(nseg, 256), 256, 0, st>>>(sums.p, t.n.p, t.p.p, nseg,
                                                             avg.p);
       CK_LAUNCH();
@@ -941,7 +1015,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
             perm.p, cent, N, t.start.p, t.n.p, t.p.p, nseg, 1, avg.p);
         CK_LAUNCH();
       }
-      seg_tree_reduce<6, GEN_INERTIA, false>(perm.p, cent, N, t, avg.p, ws, isums.p);
+      seg_tree_reduce<6, GEN_INERTIA>(perm.p, cent, N, t, avg.p, ws, isums.p);
       k_rib_axis<<<grid_for(nseg, 128), 128, 0, st>>>(
           perm.p, cent, N, t.start.p, t.n.p, t.p.p, nseg, ndim, do_local ? 1 : 0,
           avg.p, isums.p, ws.ev.p, ws.axis.p);
@@ -951,7 +1025,12 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
           ws.vals.p, ws.seg_of_elem.p);
       CK_LAUNCH();
     }
-    seg_sort_pairs(ws.keys, ws.vals, N, ws.seg_of_elem.p, nseg, ws.sort);
+    // RCB keys carry the segment id above the rank; RIB keys are full doubles
+    if (kind == BISECT_RCB)
+      seg_sort_pairs(ws.keys, ws.vals, N, nullptr, 1, ws.sort);
+    else
+      seg_sort_pairs(ws.keys, ws.vals, N, ws.seg_of_elem.p, nseg, ws.sort);
+    lg_mark(2);
     std::swap(perm.p, ws.vals.p);
     std::swap(perm.n, ws.vals.n);
     // children
@@ -962,6 +1041,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
         t.start.p, t.n.p, t.p.p, t.r0.p, nseg, do_local, ws.child_off.p, ws.t2.start.p,
         ws.t2.n.p, ws.t2.p.p, ws.t2.r0.p);
     CK_LAUNCH();
+    lg_mark(3);
     ws.t2.count = nchild;
     std::swap(t.start, ws.t2.start);
     std::swap(t.n, ws.t2.n);

@@ -38,6 +38,7 @@ struct BisectWs {
   // distinct values by rank (3 x N), built once for the centroids `rank_of`
   DBuf<u32> rank;
   DBuf<double> uniq;
+  DBuf<u32> rbox;  // per segment: min rank (3), min complemented rank (3)
   const double *rank_of = nullptr;
 };
 

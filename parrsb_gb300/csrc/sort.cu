@@ -6,10 +6,11 @@
 // the key bytes followed by the segment-id bytes; every pass is stable, so
 // ties keep their current order (the canonical tie-break).
 //
-// Per pass: a tile histogram kernel (4096 items per 256-thread CTA), a
-// per-digit exclusive scan over tiles, and a scatter kernel that ranks items
-// stably inside the CTA with __match_any_sync (warp w owns items
-// [w*512, w*512+512) of the tile, processed 32 at a time in order), stages
+// Per pass: a tile histogram kernel (4096 items per 512-thread CTA), a
+// per-digit exclusive scan over tiles, and a scatter kernel that loads its
+// 8 items per thread up front, ranks them stably inside the CTA with
+// __match_any_sync (warp w owns items [w*256, w*256+256) of the tile,
+// processed 32 at a time in order), stages
 // the tile in shared memory in digit order and writes each digit's run with
 // consecutive addresses.  One
 // up-front kernel builds the global digit histograms of every pass; passes
@@ -20,8 +21,9 @@ namespace prsb {
 
 namespace {
 
-constexpr int SORT_THREADS = 256;
-constexpr int ITEMS_PER_THREAD = 16;
+constexpr int SORT_THREADS = 512;
+constexpr int ITEMS_PER_THREAD = 8;
+constexpr int NWARP = SORT_THREADS / 32;
 constexpr int TILE = SORT_THREADS * ITEMS_PER_THREAD;  // 4096
 constexpr int MAX_PASSES = 12;                           // 8 key + 4 seg bytes
 constexpr size_t SCATTER_SMEM = (size_t)TILE * (8 + 4 + 1);  // staged keys, values, digits
@@ -65,26 +67,26 @@ __global__ void __launch_bounds__(SORT_THREADS)
 k_tile_hist(const u64 *__restrict__ keys, const int *__restrict__ vals, ll n,
             const int *__restrict__ seg_of_val, int is_seg, int shift,
             u32 *__restrict__ counts, int ntiles) {
-  __shared__ u32 h[SORT_THREADS / 32][256];
+  __shared__ u32 h[NWARP][256];
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < (SORT_THREADS / 32) * 256; i += blockDim.x)
-    (&h[0][0])[i] = 0;
+  for (int i = threadIdx.x; i < NWARP * 256; i += blockDim.x) (&h[0][0])[i] = 0;
   __syncthreads();
   ll base = (ll)blockIdx.x * TILE + warp * (32 * ITEMS_PER_THREAD);
-#pragma unroll 4
+  u32 d[ITEMS_PER_THREAD];
+#pragma unroll
   for (int r = 0; r < ITEMS_PER_THREAD; r++) {
     ll i = base + r * 32 + lane;
-    if (i < n) {
-      u32 d = digit_of(keys[i], is_seg ? vals[i] : 0, seg_of_val, is_seg, shift);
-      atomicAdd(&h[warp][d], 1u);
-    }
+    d[r] = i < n ? digit_of(keys[i], is_seg ? vals[i] : 0, seg_of_val, is_seg, shift) : 256u;
   }
+#pragma unroll
+  for (int r = 0; r < ITEMS_PER_THREAD; r++)
+    if (d[r] < 256) atomicAdd(&h[warp][d[r]], 1u);
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
+  for (int dd = threadIdx.x; dd < 256; dd += blockDim.x) {
     u32 s = 0;
 #pragma unroll
-    for (int w = 0; w < SORT_THREADS / 32; w++) s += h[w][d];
-    counts[(ll)d * ntiles + blockIdx.x] = s;
+    for (int w = 0; w < NWARP; w++) s += h[w][dd];
+    counts[(ll)dd * ntiles + blockIdx.x] = s;
   }
 }
 
@@ -135,50 +137,60 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
           const int *__restrict__ seg_of_val, int is_seg, int shift,
           const u32 *__restrict__ counts, const u32 *__restrict__ totals,
           int ntiles) {
-  constexpr int NW = SORT_THREADS / 32;
-  __shared__ u32 wcnt[NW][256];
+  __shared__ u32 wcnt[NWARP][256];
   __shared__ u32 dbase[256];
   __shared__ u32 tl[256];  // tile-local start of each digit
+  __shared__ u32 ws[8], ws2[8];
   extern __shared__ __align__(16) unsigned char sc_smem[];
   u64 *skey = reinterpret_cast<u64 *>(sc_smem);             // TILE
   int *sval = reinterpret_cast<int *>(skey + TILE);          // TILE
   unsigned char *sdig = reinterpret_cast<unsigned char *>(sval + TILE);  // TILE
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < NW * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
-  // exclusive scan of the 256 digit totals (one value per thread)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < NWARP * 256; i += blockDim.x) (&wcnt[0][0])[i] = 0;
+  // global start of every digit in this tile: exclusive scan of the 256
+  // digit totals (threads 0..255, one digit each) plus the tile's offset
   {
-    u32 v = totals[threadIdx.x];
+    const u32 v = threadIdx.x < 256 ? totals[threadIdx.x] : 0u;
     u32 x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       u32 y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    __shared__ u32 ws[NW];
-    if (lane == 31) ws[warp] = x;
+    if (threadIdx.x < 256 && lane == 31) ws[warp] = x;
     __syncthreads();
-    u32 off = 0;
-    for (int w = 0; w < warp; w++) off += ws[w];
-    dbase[threadIdx.x] = off + x - v + counts[(ll)threadIdx.x * ntiles + blockIdx.x];
+    if (threadIdx.x < 256) {
+      u32 off = 0;
+      for (int w = 0; w < warp; w++) off += ws[w];
+      dbase[threadIdx.x] = off + x - v + counts[(ll)threadIdx.x * ntiles + blockIdx.x];
+    }
   }
-  __syncthreads();
+  // every load of the tile is issued before the ranking loop
   u64 key[ITEMS_PER_THREAD];
   int val[ITEMS_PER_THREAD];
   u32 rank[ITEMS_PER_THREAD];
   u32 dig[ITEMS_PER_THREAD];
-  unsigned lt_mask = (1u << lane) - 1u;
-  ll base = (ll)blockIdx.x * TILE + warp * (32 * ITEMS_PER_THREAD);
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const ll base = (ll)blockIdx.x * TILE + warp * (32 * ITEMS_PER_THREAD);
 #pragma unroll
   for (int r = 0; r < ITEMS_PER_THREAD; r++) {
-    ll i = base + r * 32 + lane;
-    bool valid = i < n;
-    u32 d = 256;
-    if (valid) {
+    const ll i = base + r * 32 + lane;
+    if (i < n) {
       key[r] = kin[i];
       val[r] = vin[i];
-      d = digit_of(key[r], val[r], seg_of_val, is_seg, shift);
     }
-    unsigned peers = __match_any_sync(0xffffffffu, d);
+  }
+#pragma unroll
+  for (int r = 0; r < ITEMS_PER_THREAD; r++) {
+    const ll i = base + r * 32 + lane;
+    dig[r] = i < n ? digit_of(key[r], val[r], seg_of_val, is_seg, shift) : 256u;
+  }
+  // stable rank within the warp's items (32 at a time, in order)
+#pragma unroll
+  for (int r = 0; r < ITEMS_PER_THREAD; r++) {
+    const u32 d = dig[r];
+    const bool valid = d < 256;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
     u32 before = 0;
     if (valid) before = wcnt[warp][d];
     __syncwarp();
@@ -186,19 +198,20 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
       rank[r] = before + __popc(peers & lt_mask);
       if (lane == __ffs(peers) - 1) wcnt[warp][d] = before + __popc(peers);
     }
-    dig[r] = d;
     __syncwarp();
   }
   __syncthreads();
   // exclusive scan over warps per digit, then over the digits of the tile
   {
-    int d = threadIdx.x;
     u32 run = 0;
+    if (threadIdx.x < 256) {
+      const int d = threadIdx.x;
 #pragma unroll
-    for (int w = 0; w < NW; w++) {
-      u32 t = wcnt[w][d];
-      wcnt[w][d] = run;
-      run += t;
+      for (int w = 0; w < NWARP; w++) {
+        u32 t = wcnt[w][d];
+        wcnt[w][d] = run;
+        run += t;
+      }
     }
     u32 x = run;
 #pragma unroll
@@ -206,12 +219,13 @@ k_scatter(const u64 *__restrict__ kin, const int *__restrict__ vin,
       u32 y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    __shared__ u32 ws2[NW];
-    if (lane == 31) ws2[warp] = x;
+    if (threadIdx.x < 256 && lane == 31) ws2[warp] = x;
     __syncthreads();
-    u32 off = 0;
-    for (int w = 0; w < warp; w++) off += ws2[w];
-    tl[d] = off + x - run;
+    if (threadIdx.x < 256) {
+      u32 off = 0;
+      for (int w = 0; w < warp; w++) off += ws2[w];
+      tl[threadIdx.x] = off + x - run;
+    }
   }
   __syncthreads();
   // stage the tile in digit order, then write every digit run with
