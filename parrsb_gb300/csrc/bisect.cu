@@ -16,6 +16,8 @@
 
 #include "bisect.cuh"
 
+#include <type_traits>
+
 namespace prsb {
 
 namespace {
@@ -456,11 +458,15 @@ __global__ void k_rank_write(const u64 *__restrict__ keys, const int *__restrict
 // position x at depth d follows from (n, p) alone (rank split at
 // lower_count(len, p) while p > 1, then, with LOCAL, halving at len / 2 as
 // rcb_local does, src/rcb.c:39-72).  The dense ranks of the segment's
-// elements sit in shared memory for the whole recursion.  Per level:
-//   boxes   - a sequential loop for short sub-ranges, a warp-segmented min /
-//             max plus shared-memory atomics for long ones (table slot
-//             start / SMALL_SHORT: long sub-ranges are disjoint and longer
-//             than SMALL_SHORT, so their slots differ);
+// elements sit in shared memory for the whole recursion; a thread keeps the
+// sub-range of each of its positions in registers and advances it by one
+// split per level.  Per level:
+//   boxes   - a warp-segmented min / max over every round of 32 positions;
+//             a sub-range inside one round takes its axis at once, a long one
+//             (more than SMALL_SHORT) goes through shared-memory atomics
+//             (table slot start / SMALL_SHORT: long sub-ranges are disjoint
+//             and longer than SMALL_SHORT, so their slots differ), and a
+//             short one crossing a round boundary is reduced sequentially;
 //   axis    - longest edge, uniq[max] - uniq[min] per axis;
 //   order   - stable sort of each sub-range by its axis rank.  When no
 //             sub-range exceeds SMALL_CMP elements, an element's new place
@@ -476,7 +482,7 @@ constexpr int SMALL_THREADS = 1024;
 constexpr int SMALL_WARPS = SMALL_THREADS / 32;
 constexpr int SMALL_ITEMS = SMALL_MAX / SMALL_THREADS;  // positions per thread
 constexpr int SMALL_SPAN = 32 * SMALL_ITEMS;            // positions per warp
-constexpr int SMALL_CMP = 256;    // comparison ranking up to this sub-range length
+constexpr int SMALL_CMP = 64;     // comparison ranking up to this sub-range length
 constexpr int SMALL_SHORT = 32;   // sequential boxes up to this sub-range length
 constexpr int SMALL_NLONG = SMALL_MAX / SMALL_SHORT;  // box table slots
 
@@ -514,6 +520,30 @@ __device__ __forceinline__ SubR descend(int x, int n, int p0, int d) {
 template <bool LOCAL>
 __device__ __forceinline__ bool sub_active(const SubR &r) {
   return r.p > 1 || (LOCAL && r.len >= 2);
+}
+
+// lower_count for the small segments (n <= SMALL_MAX): 32-bit arithmetic
+__device__ __forceinline__ int lower_count_small(int n, int p) {
+  const int h = (p + 1) / 2;
+  const int nelt = n / p, nrem = n - p * nelt;
+  if (nrem == 0) return h * nelt;
+  const int s = p - nrem;
+  return h * nelt + (h > s ? h - s : 0);
+}
+
+// Longest box edge from rank boxes: uniq[max] - uniq[min] per axis, the
+// first strictly longest wins.
+__device__ __forceinline__ unsigned char small_axis(const double *__restrict__ uniq, ll N,
+                                                    int ndim, const u32 *mn, const u32 *mx) {
+  double l[3];
+#pragma unroll
+  for (int q = 0; q < 3; q++)
+    l[q] = q < ndim ? __dsub_rn(uniq[(ll)q * N + mx[q]], uniq[(ll)q * N + mn[q]]) : 0.0;
+  int ax = 0;
+#pragma unroll
+  for (int q = 1; q < 3; q++)
+    if (q < ndim && l[q] > l[ax]) ax = q;
+  return (unsigned char)ax;
 }
 
 // Items of k_rcb_small: local id in bits 0-15, sub-range start in bits
@@ -565,233 +595,317 @@ k_rcb_small(int *__restrict__ perm, const u32 *__restrict__ rank,
     for (int q = 0; q < ndim; q++) rk[q * SMALL_MAX + x] = rank[(ll)q * N + e];
     item[x] = (u32)x;
   }
-  const unsigned lt_mask = (1u << lane) - 1u;
-  int st_r[SMALL_ITEMS], len_r[SMALL_ITEMS];  // sub-range of each own position
-  for (int d = 0; d < 64; d++) {
-    // ---- sub-range of each position at depth d
-    if (threadIdx.x == 0) s_maxlen = 0;
-    for (int t = threadIdx.x; t < SMALL_NLONG * 6; t += blockDim.x)
-      box[t] = (t % 6) < 3 ? 0xFFFFFFFFu : 0u;
-    bool any = false;
-    int mylen = 0;
-    __syncthreads();
-#pragma unroll
+  // The level loop, instantiated for segments with one virtual rank (only
+  // the local halving, no per-position rank counts) and for the general case.
+  auto levels = [&](auto pone) {
+    constexpr bool PONE = decltype(pone)::value;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    // Sub-range of each own position at the current depth, advanced by one
+    // split per level: start | length << 16, and its virtual-rank count.
+    u32 sl_r[SMALL_ITEMS];
+    int p_r[PONE ? 1 : SMALL_ITEMS];  // with one virtual rank (PONE) p stays 1
+  #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
-      int x = warp * SMALL_SPAN + r * 32 + lane;
-      st_r[r] = -1, len_r[r] = 0;
-      if (x < n) {
-        SubR sr = descend<LOCAL>(x, n, p0, d);
-        st_r[r] = sr.st;
-        if (sub_active<LOCAL>(sr)) len_r[r] = sr.len, any = true, mylen = max(mylen, sr.len);
-      }
+      sl_r[r] = (u32)n << 16;
+      if (!PONE) p_r[r] = p0;
     }
-    if (mylen) atomicMax(&s_maxlen, mylen);
-    if (!__syncthreads_or(any)) break;
-    const int maxlen = s_maxlen;
-    // ---- bounding boxes on dense ranks, axis of each sub-range
-#pragma unroll
-    for (int r = 0; r < SMALL_ITEMS; r++) {
-      const int x = warp * SMALL_SPAN + r * 32 + lane;
-      const int st = st_r[r], len = len_r[r];
-      if (len > 0 && len <= SMALL_SHORT && st == x) {  // short: sequential
-        u32 mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
-        for (int y = x; y < x + len; y++) {
-          const u32 id = item[y] & 0xFFFFu;
-          for (int q = 0; q < ndim; q++) {
-            u32 k = rk[q * SMALL_MAX + id];
-            mn[q] = min(mn[q], k);
-            mx[q] = max(mx[q], k);
+    for (int d = 0; d < 64; d++) {
+      if (d > 0) {
+  #pragma unroll
+        for (int r = 0; r < SMALL_ITEMS; r++) {
+          const int x = warp * SMALL_SPAN + r * 32 + lane;
+          int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = PONE ? 1 : p_r[r];
+          int L, h;
+          if (p > 1) {
+            L = lower_count_small(ln, p);
+            h = (p + 1) / 2;
+          } else if (LOCAL && ln >= 2) {
+            L = ln / 2;
+            h = 0;
+          } else {
+            continue;  // finished sub-range keeps its place
           }
+          if (x < st + L) {
+            ln = L;
+            p = p > 1 ? h : p;
+          } else {
+            st += L;
+            ln -= L;
+            p = p > 1 ? p - h : p;
+          }
+          sl_r[r] = (u32)st | ((u32)ln << 16);
+          if (!PONE) p_r[r] = p;
         }
-        double best = 0.0;
-        int ax = 0;
-        for (int q = 0; q < ndim; q++) {
-          double l = __dsub_rn(uniq[(ll)q * N + mx[q]], uniq[(ll)q * N + mn[q]]);
-          if (q == 0 || l > best) best = l, ax = q;
-        }
-        sax[x] = (unsigned char)ax;
       }
-      if (maxlen > SMALL_SHORT) {  // warp-uniform
-        const bool lng = len > SMALL_SHORT;
-        const int segkey = lng ? st : -1 - lane;
-        u32 mn[3], mx[3];
-        const u32 id = lng ? (item[x] & 0xFFFFu) : 0u;
+      if (threadIdx.x == 0) s_maxlen = 0;
+      for (int t = threadIdx.x; t < SMALL_NLONG * 6; t += blockDim.x)
+        box[t] = (t % 6) < 3 ? 0xFFFFFFFFu : 0u;
+      __syncthreads();
+      u32 act_mask = 0;  // bit r: position r lies in an active sub-range
+      int mylen = 0;
+  #pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        const int ln = (int)(sl_r[r] >> 16);
+        if (x < n && ((!PONE && p_r[r] > 1) || (LOCAL && ln >= 2)))
+          act_mask |= 1u << r, mylen = max(mylen, ln);
+      }
+      if (mylen) atomicMax(&s_maxlen, mylen);
+      if (!__syncthreads_or(act_mask != 0)) break;
+      const int maxlen = s_maxlen;
+      // ---- bounding boxes on dense ranks, axis of each sub-range.  A warp
+      // whose 256 positions all lie in one active sub-range folds them per
+      // lane and reduces once; other warps reduce each round of 32 positions
+      // with a segmented shuffle tree.
+      const int st0 = (int)(sl_r[0] & 0xFFFFu);
+      bool one = act_mask == (1u << SMALL_ITEMS) - 1u;
+#pragma unroll
+      for (int r = 1; r < SMALL_ITEMS; r++) one = one && (int)(sl_r[r] & 0xFFFFu) == st0;
+      const int st0_lane0 = __shfl_sync(0xffffffffu, st0, 0);  // every lane takes part
+      const bool warp_one = __all_sync(0xffffffffu, one && st0 == st0_lane0);
+      if (warp_one) {
+        u32 mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+#pragma unroll
+        for (int r = 0; r < SMALL_ITEMS; r++) {
+          const u32 id = item[warp * SMALL_SPAN + r * 32 + lane] & 0xFFFFu;
+#pragma unroll
+          for (int q = 0; q < 3; q++)
+            if (q < ndim) {
+              const u32 k = rk[q * SMALL_MAX + id];
+              mn[q] = min(mn[q], k);
+              mx[q] = max(mx[q], k);
+            }
+        }
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-          u32 k = (lng && q < ndim) ? rk[q * SMALL_MAX + id] : 0u;
-          mn[q] = lng ? k : 0xFFFFFFFFu;
+          mn[q] = __reduce_min_sync(0xffffffffu, mn[q]);
+          mx[q] = __reduce_max_sync(0xffffffffu, mx[q]);
+        }
+        const int ln0 = (int)(sl_r[0] >> 16);
+        if (lane == 0) {
+          if (st0 == warp * SMALL_SPAN && ln0 == SMALL_SPAN) {
+            sax[st0] = small_axis(uniq, N, ndim, mn, mx);  // the whole sub-range
+          } else {  // longer than SMALL_SHORT: box table slot
+            const int o = st0 / SMALL_SHORT;
+#pragma unroll
+            for (int q = 0; q < 3; q++)
+              if (q < ndim) {
+                atomicMin(&box[6 * o + q], mn[q]);
+                atomicMax(&box[6 * o + 3 + q], mx[q]);
+              }
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const bool act = (act_mask >> r) & 1u;
+        if (warp_one || !__any_sync(0xffffffffu, act)) continue;  // warp-uniform
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16);
+        const int segkey = act ? st : -1 - lane;
+        u32 mn[3], mx[3];
+        const u32 id = act ? (item[x] & 0xFFFFu) : 0u;
+  #pragma unroll
+        for (int q = 0; q < 3; q++) {
+          const u32 k = (act && q < ndim) ? rk[q * SMALL_MAX + id] : 0u;
+          mn[q] = act ? k : 0xFFFFFFFFu;
           mx[q] = k;
         }
-#pragma unroll
+  #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-          int ok = __shfl_down_sync(0xffffffffu, segkey, off);
-          bool same = (lane + off < 32) && ok == segkey;
-#pragma unroll
+          const int ok = __shfl_down_sync(0xffffffffu, segkey, off);
+          const bool same = (lane + off < 32) && ok == segkey;
+  #pragma unroll
           for (int q = 0; q < 3; q++) {
-            u32 a2 = __shfl_down_sync(0xffffffffu, mn[q], off);
-            u32 b2 = __shfl_down_sync(0xffffffffu, mx[q], off);
+            const u32 a2 = __shfl_down_sync(0xffffffffu, mn[q], off);
+            const u32 b2 = __shfl_down_sync(0xffffffffu, mx[q], off);
             if (same) mn[q] = min(mn[q], a2), mx[q] = max(mx[q], b2);
           }
         }
-        int prevkey = __shfl_up_sync(0xffffffffu, segkey, 1);
-        bool head = lane == 0 || prevkey != segkey;
-        if (lng && head) {
-          const int o = st / SMALL_SHORT;
-          for (int q = 0; q < ndim; q++) {
-            atomicMin(&box[6 * o + q], mn[q]);
-            atomicMax(&box[6 * o + 3 + q], mx[q]);
+        const int prevkey = __shfl_up_sync(0xffffffffu, segkey, 1);
+        if (act && (lane == 0 || prevkey != segkey)) {  // first position of a run
+          const int rend = warp * SMALL_SPAN + r * 32 + 32;
+          if (x == st && st + ln <= rend) {
+            sax[st] = small_axis(uniq, N, ndim, mn, mx);  // whole sub-range in this round
+          } else if (ln > SMALL_SHORT) {
+            const int o = st / SMALL_SHORT;
+  #pragma unroll
+            for (int q = 0; q < 3; q++)
+              if (q < ndim) {
+                atomicMin(&box[6 * o + q], mn[q]);
+                atomicMax(&box[6 * o + 3 + q], mx[q]);
+              }
           }
-        }
-      }
-    }
-    __syncthreads();
-    if (maxlen > SMALL_SHORT) {
-#pragma unroll
-      for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = warp * SMALL_SPAN + r * 32 + lane;
-        if (len_r[r] > SMALL_SHORT && st_r[r] == x) {
-          const int o = x / SMALL_SHORT;
-          double best = 0.0;
-          int ax = 0;
-          for (int q = 0; q < ndim; q++) {
-            double l = __dsub_rn(uniq[(ll)q * N + box[6 * o + 3 + q]],
-                                 uniq[(ll)q * N + box[6 * o + q]]);
-            if (q == 0 || l > best) best = l, ax = q;
-          }
-          sax[x] = (unsigned char)ax;
         }
       }
       __syncthreads();
-    }
-    // ---- keys: rank along the sub-range's axis
-    u32 kand = 0xFFFFFFFFu, kor = 0u, stand = 0xFFFFFFFFu, stor = 0u;
-#pragma unroll
-    for (int r = 0; r < SMALL_ITEMS; r++) {
-      const int x = warp * SMALL_SPAN + r * 32 + lane;
-      if (x >= n) continue;
-      const u32 st = (u32)st_r[r];
-      const u32 id = item[x] & 0xFFFFu;
-      const u32 k = len_r[r] ? rk[sax[st] * SMALL_MAX + id] : 0u;
-      kx[x] = k;
-      item[x] = (st << 16) | id | (len_r[r] ? ITEM_ACTIVE : 0u);
-      kand &= k, kor |= k, stand &= st, stor |= st;
-    }
-    __syncthreads();
-    if (maxlen <= SMALL_CMP) {
-      // ---- comparison ranking inside each sub-range
-#pragma unroll
+      // sub-ranges spanning more than one round: long ones from the box table,
+      // short ones (crossing a round boundary) by a sequential loop
+  #pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16);
+        const int rend = warp * SMALL_SPAN + r * 32 + 32;
+        const bool whole_warp = st == warp * SMALL_SPAN && ln == SMALL_SPAN;
+        if (((act_mask >> r) & 1u) && x == st && st + ln > rend && !(warp_one && whole_warp)) {
+          u32 mn[3] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu}, mx[3] = {0u, 0u, 0u};
+          if (ln > SMALL_SHORT) {
+            const int o = st / SMALL_SHORT;
+  #pragma unroll
+            for (int q = 0; q < 3; q++) mn[q] = box[6 * o + q], mx[q] = box[6 * o + 3 + q];
+          } else {
+            for (int y = st; y < st + ln; y++) {
+              const u32 id = item[y] & 0xFFFFu;
+  #pragma unroll
+              for (int q = 0; q < 3; q++)
+                if (q < ndim) {
+                  const u32 k = rk[q * SMALL_MAX + id];
+                  mn[q] = min(mn[q], k);
+                  mx[q] = max(mx[q], k);
+                }
+            }
+          }
+          sax[st] = small_axis(uniq, N, ndim, mn, mx);
+        }
+      }
+      __syncthreads();
+      // ---- keys: rank along the sub-range's axis
+      u32 kand = 0xFFFFFFFFu, kor = 0u, stand = 0xFFFFFFFFu, stor = 0u;
+  #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
         const int x = warp * SMALL_SPAN + r * 32 + lane;
         if (x >= n) continue;
-        const int len = len_r[r], st = st_r[r];
-        if (!len) {
-          item2[x] = item[x];
-          continue;
-        }
-        const u32 k = kx[x];
-        int c = 0;
-        for (int y = st; y < st + len; y++) {
-          const u32 k2 = kx[y];
-          c += (k2 < k) || (k2 == k && y < x);
-        }
-        item2[st + c] = item[x];
+        const u32 st = sl_r[r] & 0xFFFFu;
+        const bool act = (act_mask >> r) & 1u;
+        const u32 id = item[x] & 0xFFFFu;
+        const u32 k = act ? rk[sax[st] * SMALL_MAX + id] : 0u;
+        kx[x] = k;
+        item[x] = (st << 16) | id | (act ? ITEM_ACTIVE : 0u);
+        kand &= k, kor |= k, stand &= st, stor |= st;
       }
       __syncthreads();
-      u32 *t = item;
-      item = item2;
-      item2 = t;
-    } else {
-      // ---- stable LSD passes over the varying bytes: rank, then start
-      if (threadIdx.x == 0) s_and = 0xFFFFFFFFu, s_or = 0u, s_stand = 0xFFFFFFFFu, s_stor = 0u;
-      __syncthreads();
-      atomicAnd(&s_and, kand);
-      atomicOr(&s_or, kor);
-      atomicAnd(&s_stand, stand);
-      atomicOr(&s_stor, stor);
-      __syncthreads();
-      const u32 kdiff = s_and ^ s_or, sdiff = s_stand ^ s_stor;
-      for (int b = 0; b < 6; b++) {
-        const bool is_st = b >= 4;
-        const int shift = is_st ? 8 * (b - 4) : 8 * b;
-        if ((((is_st ? sdiff : kdiff) >> shift) & 255u) == 0) continue;
-        for (int i = threadIdx.x; i < SMALL_WARPS * 256; i += blockDim.x) wcnt[i] = 0;
-        __syncthreads();
-        unsigned rkk[SMALL_ITEMS], dg[SMALL_ITEMS];
-        u32 itv[SMALL_ITEMS];
-#pragma unroll
+      if (maxlen <= SMALL_CMP) {
+        // ---- comparison ranking inside each sub-range
+  #pragma unroll
         for (int r = 0; r < SMALL_ITEMS; r++) {
           const int x = warp * SMALL_SPAN + r * 32 + lane;
-          unsigned dgt = 256;
-          itv[r] = 0;
-          if (x < n) {
-            const u32 it = item[x];
-            itv[r] = it;
-            // inactive positions carry key 0 (their sub-range keeps its order)
-            const u32 k = is_st ? item_st(it) : kx_key(rk, sax, it);
-            dgt = (k >> shift) & 255u;
+          if (x >= n) continue;
+          const int len = ((act_mask >> r) & 1u) ? (int)(sl_r[r] >> 16) : 0;
+          const int st = (int)(sl_r[r] & 0xFFFFu);
+          if (!len) {
+            item2[x] = item[x];
+            continue;
           }
-          unsigned peers = __match_any_sync(0xffffffffu, dgt);
-          unsigned before = 0;
-          if (dgt < 256) before = wcnt[warp * 256 + dgt];
-          __syncwarp();
-          if (dgt < 256) {
-            rkk[r] = before + __popc(peers & lt_mask);
-            if (lane == __ffs(peers) - 1)
-              wcnt[warp * 256 + dgt] = (unsigned short)(before + __popc(peers));
+          const u32 k = kx[x];
+          int c = 0;
+          for (int y = st; y < st + len; y++) {
+            const u32 k2 = kx[y];
+            c += (k2 < k) || (k2 == k && y < x);
           }
-          dg[r] = dgt;
-          __syncwarp();
-        }
-        __syncthreads();
-        if (threadIdx.x < 256) {
-          unsigned run = 0;
-          for (int w = 0; w < SMALL_WARPS; w++) {
-            unsigned t = wcnt[w * 256 + threadIdx.x];
-            wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
-            run += t;
-          }
-          dbase[threadIdx.x] = run;
-        }
-        __syncthreads();
-        if (threadIdx.x < 32) {  // exclusive scan of the 256 digit totals
-          unsigned v[8], s2 = 0;
-          for (int j = 0; j < 8; j++) v[j] = dbase[threadIdx.x * 8 + j], s2 += v[j];
-          unsigned incl = s2;
-          for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (threadIdx.x >= o) incl += y;
-          }
-          unsigned run = incl - s2;
-          for (int j = 0; j < 8; j++) dbase[threadIdx.x * 8 + j] = run, run += v[j];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < SMALL_ITEMS; r++) {
-          if (dg[r] < 256) item2[dbase[dg[r]] + wcnt[warp * 256 + dg[r]] + rkk[r]] = itv[r];
+          item2[st + c] = item[x];
         }
         __syncthreads();
         u32 *t = item;
         item = item2;
         item2 = t;
+      } else {
+        // ---- stable LSD passes over the varying bytes: rank, then start
+        if (threadIdx.x == 0) s_and = 0xFFFFFFFFu, s_or = 0u, s_stand = 0xFFFFFFFFu, s_stor = 0u;
+        __syncthreads();
+        atomicAnd(&s_and, kand);
+        atomicOr(&s_or, kor);
+        atomicAnd(&s_stand, stand);
+        atomicOr(&s_stor, stor);
+        __syncthreads();
+        const u32 kdiff = s_and ^ s_or, sdiff = s_stand ^ s_stor;
+        for (int b = 0; b < 6; b++) {
+          const bool is_st = b >= 4;
+          const int shift = is_st ? 8 * (b - 4) : 8 * b;
+          if ((((is_st ? sdiff : kdiff) >> shift) & 255u) == 0) continue;
+          for (int i = threadIdx.x; i < SMALL_WARPS * 256; i += blockDim.x) wcnt[i] = 0;
+          __syncthreads();
+          unsigned rd[SMALL_ITEMS];  // digit << 16 | rank among the warp's equal digits
+          u32 itv[SMALL_ITEMS];
+  #pragma unroll
+          for (int r = 0; r < SMALL_ITEMS; r++) {
+            const int x = warp * SMALL_SPAN + r * 32 + lane;
+            unsigned dgt = 256;
+            itv[r] = 0;
+            if (x < n) {
+              const u32 it = item[x];
+              itv[r] = it;
+              // inactive positions carry key 0 (their sub-range keeps its order)
+              const u32 k = is_st ? item_st(it) : kx_key(rk, sax, it);
+              dgt = (k >> shift) & 255u;
+            }
+            unsigned peers = __match_any_sync(0xffffffffu, dgt);
+            unsigned before = 0;
+            if (dgt < 256) before = wcnt[warp * 256 + dgt];
+            __syncwarp();
+            if (dgt < 256) {
+              rd[r] = (dgt << 16) | (before + __popc(peers & lt_mask));
+              if (lane == __ffs(peers) - 1)
+                wcnt[warp * 256 + dgt] = (unsigned short)(before + __popc(peers));
+            }
+            if (dgt >= 256) rd[r] = 256u << 16;
+            __syncwarp();
+          }
+          __syncthreads();
+          if (threadIdx.x < 256) {
+            unsigned run = 0;
+            for (int w = 0; w < SMALL_WARPS; w++) {
+              unsigned t = wcnt[w * 256 + threadIdx.x];
+              wcnt[w * 256 + threadIdx.x] = (unsigned short)run;
+              run += t;
+            }
+            dbase[threadIdx.x] = run;
+          }
+          __syncthreads();
+          if (threadIdx.x < 32) {  // exclusive scan of the 256 digit totals
+            unsigned v[8], s2 = 0;
+            for (int j = 0; j < 8; j++) v[j] = dbase[threadIdx.x * 8 + j], s2 += v[j];
+            unsigned incl = s2;
+            for (int o = 1; o < 32; o <<= 1) {
+              unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (threadIdx.x >= o) incl += y;
+            }
+            unsigned run = incl - s2;
+            for (int j = 0; j < 8; j++) dbase[threadIdx.x * 8 + j] = run, run += v[j];
+          }
+          __syncthreads();
+  #pragma unroll
+          for (int r = 0; r < SMALL_ITEMS; r++) {
+            const unsigned dgr = rd[r] >> 16;
+            if (dgr < 256) item2[dbase[dgr] + wcnt[warp * 256 + dgr] + (rd[r] & 0xFFFFu)] = itv[r];
+          }
+          __syncthreads();
+          u32 *t = item;
+          item = item2;
+          item2 = t;
+        }
       }
     }
-  }
-  // ---- write the order (and ranks) back: read every old entry, then write
-  int ev[SMALL_ITEMS];
-#pragma unroll
-  for (int r = 0; r < SMALL_ITEMS; r++) {
-    const int x = warp * SMALL_SPAN + r * 32 + lane;
-    ev[r] = x < n ? perm[start + (item[x] & 0xFFFFu)] : 0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < SMALL_ITEMS; r++) {
-    const int x = warp * SMALL_SPAN + r * 32 + lane;
-    if (x < n) {
-      perm[start + x] = ev[r];
-      if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+    // ---- write the order (and ranks) back: read every old entry, then write
+    int ev[SMALL_ITEMS];
+  #pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
+      ev[r] = x < n ? perm[start + (item[x] & 0xFFFFu)] : 0;
     }
-  }
+    __syncthreads();
+  #pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
+      if (x < n) {
+        perm[start + x] = ev[r];
+        if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+      }
+    }
+  };
+  if (p0 == 1)
+    levels(std::true_type{});
+  else
+    levels(std::false_type{});
 }
 
 __global__ void k_max_active_n(const int *__restrict__ p, const ll *__restrict__ n, ll nseg,
