@@ -40,6 +40,14 @@ void *dev_alloc(size_t bytes) {
 
 void dev_free(void *p) { cudaFreeAsync(p, ctx().stream); }
 
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *e = getenv("PARRSB_GPU_PDL");
+    return !(e && atoi(e) == 0);
+  }();
+  return on;
+}
+
 void Ctx::init() {
   if (!stream) {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));

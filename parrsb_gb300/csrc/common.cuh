@@ -6,6 +6,7 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <utility>
 #include <vector>
 
 #include "../../include/parrsb.h"
@@ -92,6 +93,34 @@ struct Ctx {
 };
 
 Ctx &ctx();
+
+// Programmatic dependent launch.  A kernel launched through launch_pdl may be
+// scheduled while its predecessor on the stream drains; its first statement,
+// pdl_entry(), waits (griddepcontrol.wait) until the predecessor grid has
+// completed and its writes are visible, so nothing is read early, and then
+// lets the next such kernel be scheduled.  For a kernel launched without the
+// attribute the wait returns at once.  PARRSB_GPU_PDL=0 launches without it.
+__device__ __forceinline__ void pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), unsigned grid, unsigned block, size_t smem,
+                       cudaStream_t st, Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr.val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = &attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  ctx().kernel_launches++;
+  CK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+}
 
 // Stage timer using CUDA events on the context stream.
 struct StageTimer {

@@ -364,6 +364,7 @@ __global__ void k_fin(GState *__restrict__ gs, int ngroups, const double *__rest
                       int it, int MI, double tol, int mpass,
                       double *__restrict__ diagT, double *__restrict__ upperT,
                       double *__restrict__ vnorm, int *__restrict__ any_active) {
+  pdl_entry();
   __shared__ double sh[32];
   int g = blockIdx.x;
   if (g >= ngroups) return;
@@ -473,6 +474,28 @@ __device__ __forceinline__ double tile_total(const double *cs, int nc) {
   return warp_tree_sum(t);
 }
 
+// FP32 kernels keep the compensated pair through the chunk and the tile:
+// the chunk value is the pair left by the fixed shuffle tree, and the tile
+// partial sums the chunk pairs (lane l: chunks l, l + 32, ... in order, then
+// the fixed tree) before one conversion to FP64.  GB300's FP64 pipe issues a
+// warp instruction about every 16 cycles per SM, so a per-chunk conversion
+// and FP64 add would cost more than the memory traffic of the chunk.
+__device__ __forceinline__ float2 chunk_pair(float s, float c) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    float s2 = __shfl_down_sync(0xffffffffu, s, off);
+    float c2 = __shfl_down_sync(0xffffffffu, c, off);
+    two_sum_pair(s, c, s2, c2);
+  }
+  return make_float2(s, c);
+}
+__device__ __forceinline__ double tile_total_pair(const float2 *cs, int nc) {
+  float s = 0.f, c = 0.f;
+  for (int q = threadIdx.x & 31; q < nc; q += 32) two_sum_pair(s, c, cs[q].x, cs[q].y);
+  const float2 t = chunk_pair(s, c);
+  return (double)t.x + (double)t.y;
+}
+
 template <typename VT, int MODE, int GATE, int FUSE>
 __global__ void __launch_bounds__(512)
 k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
@@ -480,6 +503,7 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        VT *__restrict__ V, ll N, int it, double *__restrict__ part,
        const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
        const int *__restrict__ slice_w, double *__restrict__ y64, FinArgs fa) {
+  pdl_entry();
   __shared__ double sh[32];
   __shared__ double cs[2][LZ_TILE / 32 + 1];
   int t = blockIdx.x;
@@ -619,6 +643,7 @@ struct LaneSum {
   VT s = (VT)0, c = (VT)0;
   __device__ __forceinline__ void add(const Term<VT> &t);
   __device__ __forceinline__ double chunk() const;
+  __device__ __forceinline__ float2 pair() const { return chunk_pair((float)s, (float)c); }
 };
 template <>
 __device__ __forceinline__ void LaneSum<float>::add(const Term<float> &t) {
@@ -649,11 +674,13 @@ __global__ void __launch_bounds__(512)
 k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
      GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
      VT *__restrict__ V, ll N, double *__restrict__ part, FinArgs fa) {
+  pdl_entry();
   using Vec = VecOf<VT>;
   constexpr int R = Vec::R, CH = 32 * R;
   constexpr int OP = MODE == TM_P ? FIN_PMEAN : FIN_RTR;
   __shared__ double sh[32];
   __shared__ double cs[LZ_TILE / CH + 2];
+  __shared__ float2 cs2[LZ_TILE / CH + 2];  // chunk pairs (FP32)
   const int t = blockIdx.x;
   const int g = tgrp[t];
   const GState &s = gs[g];
@@ -695,13 +722,18 @@ k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__rest
         if (i0[u] + k >= b && i0[u] + k < e) acc.add(tv);
       }
       store_rows(MODE == TM_P ? p : rn, i0[u], b, e, o);
-      double v = acc.chunk();
-      if (lane == 0) cs[q0 + u] = v;
+      if constexpr (sizeof(VT) == 4) {
+        const float2 v = acc.pair();
+        if (lane == 0) cs2[q0 + u] = v;
+      } else {
+        const double v = acc.chunk();
+        if (lane == 0) cs[q0 + u] = v;
+      }
     }
   }
   __syncthreads();
   if (threadIdx.x < 32) {
-    double v0 = tile_total(cs, nc);
+    const double v0 = sizeof(VT) == 4 ? tile_total_pair(cs2, nc) : tile_total(cs, nc);
     if (threadIdx.x == 0) part[t] = v0;
   }
   if (FUSE) fused_fin<OP>(gs, g, part, fa, sh);
@@ -732,8 +764,10 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
        const int *__restrict__ slice_w, const VT *__restrict__ p, VT *__restrict__ w,
        double *__restrict__ part, FinArgs fa, int fuse, int force) {
+  pdl_entry();
   __shared__ double sh[32];
   __shared__ double cs[LZ_TILE / 32 + 1];
+  __shared__ float2 cs2[LZ_TILE / 32 + 1];  // chunk pairs (FP32)
   __shared__ double wlut[16];
   if (threadIdx.x < 16) wlut[threadIdx.x] = (double)threadIdx.x;
   __syncthreads();
@@ -803,12 +837,17 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
       w[i] = y;
       tv.set_prod(y, pi - c);
     }
-    double v = tv.chunk();
-    if (lane == 0) cs[q] = v;
+    if constexpr (sizeof(VT) == 4) {
+      const float2 v = chunk_pair(tv.s, tv.c);
+      if (lane == 0) cs2[q] = v;
+    } else {
+      const double v = tv.chunk();
+      if (lane == 0) cs[q] = v;
+    }
   }
   __syncthreads();
   if (threadIdx.x < 32) {
-    double v0 = tile_total(cs, nc);
+    const double v0 = sizeof(VT) == 4 ? tile_total_pair(cs2, nc) : tile_total(cs, nc);
     if (threadIdx.x == 0) part[t] = v0;
   }
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
@@ -877,9 +916,10 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
            const int *__restrict__ slice_w, const float *__restrict__ p, float *__restrict__ w,
            double *__restrict__ part, FinArgs fa, int fuse, int force, int stage_bytes,
            int *__restrict__ err) {
+  pdl_entry();
   extern __shared__ __align__(128) unsigned char sp_smem[];
   __shared__ double sh[32];
-  __shared__ double cs[LZ_TILE / 32 + 1];
+  __shared__ float2 cs[LZ_TILE / 32 + 1];  // chunk pairs
   __shared__ ll soff[LZ_TILE / 32 + 2];
   __shared__ __align__(8) unsigned long long bars[SP_NST];
   __shared__ int s_bad;
@@ -951,16 +991,16 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         w[i] = sum;
         tv.set_prod(sum, pi - c);
       }
-      double v = tv.chunk();
+      const float2 v = chunk_pair(tv.s, tv.c);
       if (lane == 0) cs[q] = v;
     } else if (q < nc && lane == 0) {
-      cs[q] = 0.0;
+      cs[q] = make_float2(0.f, 0.f);
     }
     __syncthreads();  // buffer j % SP_NST is free again
     if (threadIdx.x == 0 && j + SP_NST < nst) issue(j + SP_NST);
   }
   if (threadIdx.x < 32) {
-    double v0 = tile_total(cs, nc);
+    const double v0 = tile_total_pair(cs, nc);
     if (threadIdx.x == 0) {
       if (s_bad) atomicExch(err, 1);
       part[t] = v0;
@@ -980,6 +1020,7 @@ k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
        const int *__restrict__ tgrp, const GState *__restrict__ gs,
        const VT *__restrict__ V, ll N, const double *__restrict__ coef, int MI,
        VT *__restrict__ f, double *__restrict__ part) {
+  pdl_entry();
   using Vec = VecOf<VT>;
   constexpr int R = Vec::R, CH = 32 * R;
   __shared__ double cf[MAX_MITER];
@@ -1236,6 +1277,7 @@ __device__ double eig_index(const double *d, const double *e2, int n, int k, dou
 __global__ void k_tri_eig(GState *__restrict__ gs, int ngroups,
                           const double *__restrict__ diagT, const double *__restrict__ upperT,
                           const double *__restrict__ vnorm, int MI, double *__restrict__ coef) {
+  pdl_entry();
   extern __shared__ double eig_sm[];
   const int g = blockIdx.x, lane = threadIdx.x;
   if (g >= ngroups) return;
@@ -1382,7 +1424,13 @@ struct Lanczos {
       const char *v2 = getenv("PARRSB_GPU_SPMV_FUSED");
       sp_fused = v2 && atoi(v2) != 0;
     }
-    pr_bd = vec_threads<VT>(max_tile, pr_u);
+    // FP32: four warps per block (fewer tiles per SM wait on one block's
+    // reduction tail; measured fastest on 8M-row levels); the chunk order of
+    // the reduction does not depend on the block size
+    pr_bd = sizeof(VT) == 4 ? std::min(vec_threads<VT>(max_tile, pr_u), 128)
+                            : vec_threads<VT>(max_tile, pr_u);
+    if (const char *v = getenv("PARRSB_GPU_PR_THREADS"))  // 32..512, a multiple of 32
+      pr_bd = std::max(32, std::min(512, atoi(v) / 32 * 32));
     ritz_bd = vec_threads<VT>(max_tile, 1);
     VS = (N + 63) & ~(ll)63;
     gs.ensure(A);
@@ -1425,17 +1473,15 @@ struct Lanczos {
 
   template <int MODE, int GATE, int FUSE = -1>
   void tile(int it = 0, const Level *lv = nullptr, double tol = 0.0, int mpass = 0) {
-    k_tile<VT, MODE, GATE, FUSE><<<T, bd, 0, ctx().stream>>>(
-        tbeg.p, tend.p, tgrp.p, gs.p, f.p, V.p, N, it, part.p,
-        lv ? lv->ell.p : nullptr, lv ? lv->slice_off.p : nullptr,
-        lv ? lv->slice_w.p : nullptr, y64.p, fargs(it, tol, mpass));
-    CK_LAUNCH();
+    launch_pdl(k_tile<VT, MODE, GATE, FUSE>, T, bd, 0, ctx().stream, tbeg.p, tend.p, tgrp.p,
+               gs.p, f.p, V.p, N, it, part.p, lv ? lv->ell.p : nullptr,
+               lv ? lv->slice_off.p : nullptr, lv ? lv->slice_w.p : nullptr, y64.p,
+               fargs(it, tol, mpass));
   }
   template <int OP, int GATE>
   void fin(int it = 0, double tol = 0.0, int mpass = 0) {
-    k_fin<OP, GATE><<<A, LZ_THREADS, 0, ctx().stream>>>(gs.p, A, part.p, it, MI, tol, mpass,
-                                                        diagT.p, upperT.p, vnorm.p, any.p);
-    CK_LAUNCH();
+    launch_pdl(k_fin<OP, GATE>, A, LZ_THREADS, 0, ctx().stream, gs.p, A, part.p, it, MI, tol,
+               mpass, diagT.p, upperT.p, vnorm.p, any.p);
   }
 
   void initial_vector() {
@@ -1467,13 +1513,12 @@ struct Lanczos {
       // last tile block of the group
       mark(4 * it + 0);
       if (pr_fused) {
-        (pr_u == 4 ? k_pr<VT, TM_P, 4> : k_pr<VT, TM_P, 1>)<<<T, pr_bd, 0, st>>>(
-            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-        CK_LAUNCH();
+        launch_pdl(pr_u == 4 ? k_pr<VT, TM_P, 4> : k_pr<VT, TM_P, 1>, T, pr_bd, 0, st, tbeg.p,
+                   tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
       } else {  // tile partials, then one block per group
-        (pr_u == 4 ? k_pr<VT, TM_P, 4, false> : k_pr<VT, TM_P, 1, false>)<<<T, pr_bd, 0, st>>>(
-            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-        CK_LAUNCH();
+        launch_pdl(pr_u == 4 ? k_pr<VT, TM_P, 4, false> : k_pr<VT, TM_P, 1, false>, T, pr_bd, 0,
+                   st, tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p,
+                   fargs(it, tol, mpass));
         fin<FIN_PMEAN, GATE_RUN>(it, tol, mpass);
       }
       mark(4 * it + 1);
@@ -1484,25 +1529,22 @@ struct Lanczos {
       (*spmv_launches)++;
       mark(4 * it + 2);
       if (pr_fused) {
-        (pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>)<<<T, pr_bd, 0, st>>>(
-            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-        CK_LAUNCH();
+        launch_pdl(pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>, T, pr_bd, 0, st, tbeg.p,
+                   tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
       } else {
-        (pr_u == 4 ? k_pr<VT, TM_R, 4, false> : k_pr<VT, TM_R, 1, false>)<<<T, pr_bd, 0, st>>>(
-            tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
-        CK_LAUNCH();
+        launch_pdl(pr_u == 4 ? k_pr<VT, TM_R, 4, false> : k_pr<VT, TM_R, 1, false>, T, pr_bd, 0,
+                   st, tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p,
+                   fargs(it, tol, mpass));
         fin<FIN_RTR, GATE_RUN>(it, tol, mpass);
       }
       mark(4 * it + 3);
     }
     mark(4 * MI + 2);
-    k_tri_eig<<<A, 32, eig_smem(), st>>>(gs.p, A, diagT.p, upperT.p, vnorm.p, MI, coef.p);
-    CK_LAUNCH();
+    launch_pdl(k_tri_eig, A, 32, eig_smem(), st, gs.p, A, diagT.p, upperT.p, vnorm.p, MI, coef.p);
     mark(4 * MI + 3);
     mark(4 * MI + 4);
-    k_ritz<VT><<<T, ritz_bd, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, V.p, VS, coef.p, MI,
-                                         f.p, part.p);
-    CK_LAUNCH();
+    launch_pdl(k_ritz<VT>, T, ritz_bd, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, V.p, VS, coef.p, MI,
+               f.p, part.p);
     mark(4 * MI + 5);
     fin<FIN_RITZ_MEAN, GATE_ACTIVE>();
     tile<TM_SUB_C, GATE_ACTIVE>();
@@ -1520,15 +1562,13 @@ struct Lanczos {
     cudaStream_t st = ctx().stream;
     if (kind == 1 && sizeof(VT) == 4) {
       const size_t sb = sp_stage_bytes(lv, threads);
-      k_spmv_tma<<<T, threads, SP_NST * sb, st>>>(
-          tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p,
-          reinterpret_cast<const float *>(p.p), reinterpret_cast<float *>(w.p), part.p, fa, fuse,
-          force, (int)sb, err.p);
+      launch_pdl(k_spmv_tma, T, threads, SP_NST * sb, st, tbeg.p, tend.p, tgrp.p, gs.p,
+                 lv.ell.p, lv.slice_off.p, lv.slice_w.p, reinterpret_cast<const float *>(p.p),
+                 reinterpret_cast<float *>(w.p), part.p, fa, fuse, force, (int)sb, err.p);
     } else {
-      k_spmv<VT><<<T, threads, 0, st>>>(tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p, lv.slice_off.p,
-                                        lv.slice_w.p, p.p, w.p, part.p, fa, fuse, force);
+      launch_pdl(k_spmv<VT>, T, threads, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, lv.ell.p,
+                 lv.slice_off.p, lv.slice_w.p, p.p, w.p, part.p, fa, fuse, force);
     }
-    CK_LAUNCH();
   }
 
   // Autotuner: threads per tile block for this level.  Candidates are timed
