@@ -73,61 +73,102 @@ __global__ void k_scatter_inv(const int *__restrict__ vals, ll n, int *__restric
   if (i < n) inv[vals[i]] = (int)i;
 }
 
-// Row a of the dual graph.  Neighbour b is reached through every vertex slot
-// it shares with a; it is emitted once, from the lowest slot k of a whose
-// vertex b contains and from b's lowest slot carrying that vertex.
+// Dual-graph rows, one warp per element a (src/con.c's element graph: two
+// elements are adjacent when they share a vertex, weighted by the number of
+// shared vertex pairs).  The candidates of a are the elements of the runs of
+// its vertices, vertex by vertex, each run in slot order; an element b != a
+// occurs once per (vertex of a, equal vertex of b) pair, so its weight is its
+// number of occurrences, and the row lists every b at its first occurrence.
+// Up to GR_CAP candidates sit in shared memory; a longer list is read from
+// the runs again.  FILL = false: row lengths and the largest weight;
+// FILL = true: columns and weights at rowptr[a].
+constexpr int GR_WARPS = 4;
+constexpr int GR_CAP = 256;
+
 template <bool FILL>
-__global__ void k_graph_rows(const long long *__restrict__ vtx, int nv, ll N,
-                             const int *__restrict__ sorted_slot,
-                             const int *__restrict__ inv, const int *__restrict__ runid,
-                             const ll *__restrict__ run_start,
-                             const ll *__restrict__ rowptr, int *__restrict__ col,
-                             unsigned char *__restrict__ wout, ll *__restrict__ rowlen,
-                             int *__restrict__ maxw) {
-  const ll a = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(GR_WARPS * 32)
+k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__restrict__ inv,
+             const int *__restrict__ runid, const ll *__restrict__ run_start,
+             const ll *__restrict__ rowptr, int *__restrict__ col,
+             unsigned char *__restrict__ wout, ll *__restrict__ rowlen, int *__restrict__ maxw) {
+  __shared__ __align__(16) int cand[GR_WARPS][GR_CAP + 4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const ll a = (ll)blockIdx.x * GR_WARPS + wid;
   int wmax = 0;
-  if (a < N) {
-    long long va[8];
-    for (int k = 0; k < nv; k++) va[k] = vtx[a * nv + k];
-    ll cnt = 0, out = FILL ? rowptr[a] : 0;
-    for (int k = 0; k < nv; k++) {
-      int r = runid[inv[a * nv + k]];
-      for (ll q = run_start[r]; q < run_start[r + 1]; q++) {
-        int slot = sorted_slot[q];
-        ll b = slot / nv;
-        if (b == a) continue;
-        int l = slot - (int)b * nv;
-        long long vb[8];
-        for (int m = 0; m < nv; m++) vb[m] = vtx[b * nv + m];
-        bool first = true;
-        for (int kk = 0; kk < k && first; kk++)
-          for (int m = 0; m < nv; m++)
-            if (vb[m] == va[kk]) {
-              first = false;
-              break;
-            }
-        for (int m = 0; m < l && first; m++)
-          if (vb[m] == va[k]) first = false;
-        if (!first) continue;
-        int wt = 0;
-        for (int kk = 0; kk < nv; kk++)
-          for (int m = 0; m < nv; m++) wt += (va[kk] == vb[m]);
-        if (FILL) {
-          col[out + cnt] = (int)b;
-          wout[out + cnt] = (unsigned char)(wt > 255 ? 255 : wt);
-        }
-        if (wt > wmax) wmax = wt;
-        cnt++;
-      }
+  if (a < N) {  // warp-uniform
+    // run of each vertex of a (lane k < nv), then every lane holds all of them
+    ll rs = 0, rl = 0;
+    if (lane < nv) {
+      const int r = runid[inv[a * nv + lane]];
+      rs = run_start[r];
+      rl = run_start[r + 1] - rs;
     }
-    if (!FILL) rowlen[a] = cnt;
+    ll RS[8], EX[8];
+    ll C = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      RS[k] = __shfl_sync(0xffffffffu, rs, k);
+      EX[k] = C;
+      C += __shfl_sync(0xffffffffu, rl, k);  // lanes >= nv hold 0
+    }
+    auto cand_at = [&](ll t) -> int {  // element of candidate t
+      ll base = RS[0] - EX[0];
+#pragma unroll
+      for (int k = 1; k < 8; k++)
+        if (k < nv && t >= EX[k]) base = RS[k] - EX[k];
+      return sorted_slot[base + t] / nv;
+    };
+    const bool staged = C <= GR_CAP;
+    if (staged) {  // padded to a multiple of four with -2 (never an element)
+      for (ll t = lane; t < ((C + 3) & ~3ll); t += 32) cand[wid][t] = t < C ? cand_at(t) : -2;
+      __syncwarp();
+    }
+    ll out = 0;
+    for (ll t0 = 0; t0 < C; t0 += 32) {
+      const ll t = t0 + lane;
+      bool first = false;
+      int b = -1, cnt = 0;
+      if (t < C) {
+        b = staged ? cand[wid][t] : cand_at(t);
+        if (b != (int)a) {
+          int before = 0;  // occurrences of b ahead of t
+          if (staged) {
+            const int4 *c4 = reinterpret_cast<const int4 *>(cand[wid]);
+            for (int j = 0; j < (int)C; j += 4) {
+              const int4 v = c4[j >> 2];
+              const int m0 = v.x == b, m1 = v.y == b, m2 = v.z == b, m3 = v.w == b;
+              cnt += m0 + m1 + m2 + m3;
+              before += (m0 & (j < t)) + (m1 & (j + 1 < t)) + (m2 & (j + 2 < t)) +
+                        (m3 & (j + 3 < t));
+            }
+          } else {
+            for (ll j = 0; j < C; j++) {
+              const int m = cand_at(j) == b;
+              cnt += m;
+              before += m & (j < t);
+            }
+          }
+          first = before == 0;
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, first);
+      if (first) {
+        if (FILL) {
+          const ll pos = rowptr[a] + out + __popc(m & lt);
+          col[pos] = b;
+          wout[pos] = (unsigned char)(cnt > 255 ? 255 : cnt);
+        }
+        wmax = max(wmax, cnt);
+      }
+      out += __popc(m);
+    }
+    if (!FILL && lane == 0) rowlen[a] = out;
   }
-  if (!FILL) {
-    // one atomic per warp (every lane reaches this shuffle): a global atomic
-    // per row serialises on one address
+  if (!FILL) {  // one atomic per warp; every lane reaches the shuffles
     for (int off = 16; off > 0; off >>= 1)
       wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, off));
-    if ((threadIdx.x & 31) == 0) atomicMax(maxw, wmax);
+    if (lane == 0 && wmax) atomicMax(maxw, wmax);
   }
 }
 
@@ -2098,9 +2139,9 @@ void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g, SortWs &
   DBuf<int> maxw(1);
   CK(cudaMemsetAsync(maxw.p, 0, sizeof(int), st));
   CK(cudaMemsetAsync(rowlen.p + nel, 0, sizeof(ll), st));
-  k_graph_rows<false><<<grid_for(nel, 128), 128, 0, st>>>(
-      d_vtx, nv, nel, vals.p, inv.p, runid.p, run_start.p, nullptr, nullptr, nullptr,
-      rowlen.p, maxw.p);
+  const unsigned gr_blocks = grid_for(nel, GR_WARPS);
+  k_graph_rows<false><<<gr_blocks, GR_WARPS * 32, 0, st>>>(
+      nv, nel, vals.p, inv.p, runid.p, run_start.p, nullptr, nullptr, nullptr, rowlen.p, maxw.p);
   CK_LAUNCH();
   g.nnz = exclusive_scan_ll(rowlen.p, g.rowptr.p, nel + 1);
   DBuf<unsigned long long> mrow(1);
@@ -2116,9 +2157,9 @@ void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g, SortWs &
   g.max_w = hw;
   g.col.ensure((size_t)g.nnz + 1);
   g.w.ensure((size_t)g.nnz + 1);
-  k_graph_rows<true><<<grid_for(nel, 128), 128, 0, st>>>(
-      d_vtx, nv, nel, vals.p, inv.p, runid.p, run_start.p, g.rowptr.p, g.col.p, g.w.p,
-      nullptr, nullptr);
+  k_graph_rows<true><<<gr_blocks, GR_WARPS * 32, 0, st>>>(
+      nv, nel, vals.p, inv.p, runid.p, run_start.p, g.rowptr.p, g.col.p, g.w.p, nullptr,
+      nullptr);
   CK_LAUNCH();
 }
 
