@@ -236,6 +236,28 @@ def test_rsb_staged_spmv_bitwise(monkeypatch, shape, nparts):
 
 
 
+@pytest.mark.parametrize("partitioner", [0, 1])
+def test_pinned_host_buffers_same_partition(partitioner):
+    """parrsb_part_mesh with page-locked host buffers, called twice on the
+    same workspace, gives bitwise the partition of pageable buffers."""
+    import ctypes
+    import torch
+    from parrsb_gb300.options import ParrsbOptions
+    vtx, xyz = meshgen.box_hex(24, 20, 16, jitter=0.1, seed=5)
+    ref = P.part_mesh(vtx, xyz, 12, partitioner=partitioner)
+    h_vtx = torch.from_numpy(np.ascontiguousarray(vtx)).pin_memory()
+    h_xyz = torch.from_numpy(np.ascontiguousarray(xyz)).pin_memory()
+    h_part = torch.full((len(vtx),), -1, dtype=torch.int32).pin_memory()
+    o = ParrsbOptions.make(partitioner=partitioner, verbose_level=0)
+    for _ in range(2):  # the second call reuses the workspace buffers
+        rc = P.library().parrsb_part_mesh(ctypes.c_void_p(h_part.data_ptr()),
+                                          ctypes.c_void_p(h_vtx.data_ptr()),
+                                          ctypes.c_void_p(h_xyz.data_ptr()), None, len(vtx), 8,
+                                          ctypes.byref(o), 12)
+        assert rc == 0
+        np.testing.assert_array_equal(h_part.numpy(), ref)
+
+
 # -------------------------------------------------------- periodic gencon
 @pytest.mark.parametrize("shape", [(5, 4, 3), (32, 24, 16), (7, 1, 1)])
 def test_gencon_periodic_hex_bit_exact(oracle, shape):
