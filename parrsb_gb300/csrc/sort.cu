@@ -10,9 +10,8 @@
 // per-digit exclusive scan over tiles, and a scatter kernel that loads its
 // 8 items per thread up front, ranks them stably inside the CTA with
 // __match_any_sync (warp w owns items [w*256, w*256+256) of the tile,
-// processed 32 at a time in order), stages
-// the tile in shared memory in digit order and writes each digit's run with
-// consecutive addresses.  One
+// processed 32 at a time in order), stages the tile in shared memory in
+// digit order and writes each digit's run with consecutive addresses.  One
 // up-front kernel builds the global digit histograms of every pass; passes
 // whose digit is constant over all items are skipped.
 #include "sort.cuh"
