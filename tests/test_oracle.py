@@ -290,3 +290,53 @@ def test_oracle_periodic_quad_and_errors(oracle):
     _, xyz3 = meshgen.box_hex(5, 4, 3, jitter=0.1, seed=2)
     rc, _, _, _ = oracle.conn_mesh(xyz3, 3, 0.2, periodic=[(1, 4, 27, 2), (27, 2, 1, 4)])
     assert rc == 3  # faces do not coincide
+
+
+def _rows_by_occurrence(vtx):
+    """The GPU dual-graph rows' enumeration, restated in numpy: slots sorted
+    stably by vertex id; the candidates of element a are the runs of its
+    vertices, vertex by vertex; b's weight is its number of occurrences and
+    it is listed at its first occurrence."""
+    nel, nv = vtx.shape
+    flat = vtx.reshape(-1)
+    order = np.argsort(flat, kind="stable")  # sorted slots
+    sorted_ids = flat[order]
+    starts = np.flatnonzero(np.r_[True, sorted_ids[1:] != sorted_ids[:-1]])
+    ends = np.r_[starts[1:], len(flat)]
+    run_of_pos = np.repeat(np.arange(len(starts)), ends - starts)
+    pos_of_slot = np.empty_like(order)
+    pos_of_slot[order] = np.arange(len(order))
+    rows = []
+    for a in range(nel):
+        cand = []
+        for k in range(nv):
+            r = run_of_pos[pos_of_slot[a * nv + k]]
+            cand.extend((order[starts[r]:ends[r]] // nv).tolist())
+        seen, row = {}, []
+        for b in cand:
+            if b == a:
+                continue
+            if b not in seen:
+                seen[b] = 0
+                row.append(b)
+            seen[b] += 1
+        rows.append([(b, seen[b]) for b in row])
+    return rows
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_dual_graph_weights_are_run_occurrences(oracle, seed):
+    """Counting an element's occurrences in the vertex runs of another gives
+    the number of equal (corner, corner) pairs, repeated vertex ids inside
+    an element included: the rows equal the oracle's dual graph."""
+    rng = np.random.default_rng(seed)
+    nel, nv = 60, 8
+    vtx = rng.integers(1, 90, size=(nel, nv)).astype(np.int64)  # repeats within elements
+    rowptr, col, w = oracle.dual_graph(vtx)
+    rows = _rows_by_occurrence(vtx)
+    for a in range(nel):
+        want = dict(zip(col[rowptr[a]:rowptr[a + 1]].tolist(),
+                        w[rowptr[a]:rowptr[a + 1]].tolist()))
+        got = dict(rows[a])
+        assert got == want, a
+        assert len(rows[a]) == len(got)  # each neighbour listed once
