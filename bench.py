@@ -348,14 +348,26 @@ def main():
     os.environ["PARRSB_GPU_TIMING"] = "0"
     # ---- end to end (host buffers, copies inside the timed region)
     t_e2e = None
+    e2e_stages = None
     if not args.no_e2e:
         step_host()
         barrier()
         t0 = time.perf_counter()
+        per_call = []
         for _ in range(args.steps):
-            step_host()
+            se = step_host()
+            per_call.append((se.stage_ms[0], se.stage_ms[9], se.total_ms,
+                             sum(se.stage_ms[1:9])))
         barrier()
         t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
+        # where the host-buffer call spends its time, median and max over the
+        # timed calls: H2D copy, D2H copy, the whole call (host clock), and
+        # the device stages in between
+        e2e_stages = {}
+        for k, name in enumerate(["upload_ms", "download_ms", "call_ms", "device_stages_ms"]):
+            xs = [c[k] for c in per_call]
+            e2e_stages[name] = round(statistics.median(xs), 2)
+            e2e_stages[name.replace("_ms", "_max_ms")] = round(max(xs), 2)
         part = h_part.numpy().copy()
     else:
         part = d_part.cpu().numpy()
@@ -431,7 +443,7 @@ def main():
                    "l2": "inputs (2.1 GB mesh) larger than L2",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(part.nbytes)},
+                "d2h_bytes_per_step": int(part.nbytes), "last_call": e2e_stages},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": tr_val, "kernel": "k_spmv (sliced-ELL Laplacian)",

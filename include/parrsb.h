@@ -11,6 +11,9 @@
  * All pointers are caller-owned HOST memory unless an entry point's name
  * ends in `_device`, in which case they are device pointers on the current
  * CUDA device.  Outputs are written only on success (return value 0).
+ * Every call runs on the CUDA device that is current when it is made; the
+ * library keeps one stream and one cached workspace per host thread and
+ * device, so a thread may change device between calls.
  *
  * Return codes (the reference returns 0 / 1 / the gencon check error and
  * otherwise aborts the process; this library never exits):
@@ -203,6 +206,27 @@ PARRSB_API int parrsb_fiedler_groups(double *fiedler, long long *iters, double *
 PARRSB_API int parrsb_part_quality(double *q, const int *part, const long long *vtx,
                         int nel, int nv, int nparts);
 
+/* The element dual graph that RSB's Laplacian is built on (two elements are
+ * adjacent when they share a vertex id; the weight is the number of
+ * (corner, corner) pairs with equal ids), built on the GPU: the matrix of
+ * gs_weighted_init / gs_weighted (src/laplacian.c:159-205) and of the CSR
+ * Laplacian (src/mat.c:17-61), without the diagonal.  rowptr[nel + 1] is
+ * always written and *nnz receives the number of entries; col / weight
+ * (0-based element index, weight) are written, row by row with each row in
+ * the order of its first shared vertex, when neither is NULL and
+ * cap >= *nnz.  Host arrays. */
+PARRSB_API int parrsb_dual_graph(long long *rowptr, int *col, unsigned char *weight,
+                                 long long *nnz, long long cap, const long long *vtx, int nel,
+                                 int nv);
+
+/* Number of vertex-connected components of each group of elements
+ * (get_components_v2, src/components.c:160-328, count only): group[e] in
+ * [0, ngroups), or negative to leave element e out; ncomp[g] receives the
+ * count of group g (0 for an empty group).  The same GPU kernels as the
+ * component check of each bisection.  Host arrays. */
+PARRSB_API int parrsb_components(int *ncomp, const long long *vtx, const int *group, int nel,
+                                 int nv, int ngroups);
+
 /* Release the device workspace cached by earlier calls on this thread. */
 PARRSB_API void parrsb_gpu_finalize(void);
 
@@ -223,7 +247,10 @@ PARRSB_API void parrsb_gpu_finalize(void);
  * address and sets a kernel attribute; make it before any stream capture.
  * The scratch is shared by every call on a device: calls that overlap in
  * time (other streams, other threads) race on it and must be serialised by
- * the caller. */
+ * the caller.  The call returns before its kernels finish, so two calls made
+ * one after the other on the host but on different streams also overlap on
+ * the device: order them (cudaEventRecord on the first stream, then
+ * cudaStreamWaitEvent on the second) or use one stream. */
 PARRSB_API int parrsb_part_mesh_rcb_noalloc(int *d_part, const double *d_xyz, int nel, int nv,
                                             int nparts, void *stream);
 

@@ -30,7 +30,7 @@ EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
            "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
            "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq",
            "parrsb_read_mesh", "parrsb_dump_con", "parrsb_dump_map",
-           "parrsb_part_mesh_rcb_noalloc"]
+           "parrsb_part_mesh_rcb_noalloc", "parrsb_dual_graph", "parrsb_components"]
 
 
 class ParrsbError(RuntimeError):
@@ -113,6 +113,11 @@ def library(build_if_missing=False):
     L.parrsb_gpu_finalize.restype = None
     L.parrsb_part_mesh_rcb_noalloc.argtypes = [P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P]
     L.parrsb_part_mesh_rcb_noalloc.restype = ctypes.c_int
+    L.parrsb_dual_graph.argtypes = [P, P, P, P, ctypes.c_longlong, P, ctypes.c_int,
+                                    ctypes.c_int]
+    L.parrsb_dual_graph.restype = ctypes.c_int
+    L.parrsb_components.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.parrsb_components.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -219,6 +224,39 @@ def fiedler_groups(vtx, group, ngroups, batched=True, **kw):
     return f, it, rs
 
 
+def dual_graph(vtx):
+    """The element dual graph built on the GPU (parrsb_dual_graph): (rowptr,
+    col, weight), each row's columns in first-occurrence order."""
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    nel, nv = vtx.shape
+    rowptr = np.zeros(nel + 1, np.int64)
+    nnz = ctypes.c_longlong(0)
+    rc = library().parrsb_dual_graph(_ptr(rowptr), None, None, ctypes.byref(nnz), 0, _ptr(vtx),
+                                     nel, nv)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_dual_graph")
+    col = np.zeros(max(nnz.value, 1), np.int32)
+    w = np.zeros(max(nnz.value, 1), np.uint8)
+    rc = library().parrsb_dual_graph(_ptr(rowptr), _ptr(col), _ptr(w), ctypes.byref(nnz),
+                                     len(col), _ptr(vtx), nel, nv)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_dual_graph")
+    return rowptr, col[:nnz.value], w[:nnz.value]
+
+
+def components(vtx, group, ngroups):
+    """Vertex-connected components per group, on the GPU (parrsb_components);
+    group[e] < 0 leaves element e out."""
+    vtx = np.ascontiguousarray(vtx, np.int64)
+    group = np.ascontiguousarray(group, np.int32)
+    out = np.zeros(ngroups, np.int32)
+    rc = library().parrsb_components(_ptr(out), _ptr(vtx), _ptr(group), len(vtx), vtx.shape[1],
+                                     ngroups)
+    if rc != OK:
+        raise ParrsbError(rc, "parrsb_components")
+    return out
+
+
 _libc = None
 
 
@@ -307,6 +345,7 @@ def finalize():
 
 __all__ = ["part_mesh", "part_mesh_seq", "conn_mesh", "read_mesh", "dump_con",
            "dump_map", "write_re2", "part_quality", "last_stats", "fiedler_groups",
+           "dual_graph", "components",
            "default_options", "ParrsbOptions", "ParrsbError", "DEFAULTS",
            "library", "finalize", "OK", "ERR_ARGS", "ERR_CUDA", "ERR_CHECK",
            "ERR_UNSUPPORTED"]

@@ -49,15 +49,18 @@ bool pdl_enabled() {
 }
 
 void Ctx::init() {
-  if (!stream) {
-    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= MAX_DEVICES) throw ArgError{PARRSB_ERR_UNSUPPORTED, "device index >= 64"};
+  if (!streams[dev]) {
+    CK(cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking));
     cudaMemPool_t pool;
     CK(cudaDeviceGetDefaultMemPool(&pool, dev));
     unsigned long long keep = ~0ull;  // keep freed blocks for reuse
     CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
   }
+  device = dev;
+  stream = streams[dev];
   memset(&stats, 0, sizeof(stats));
   kernel_launches = 0;
   const char *t = getenv("PARRSB_GPU_TIMING");
@@ -73,10 +76,13 @@ struct Workspace {
   DBuf<int> part;
   DBuf<long long> ids;
 };
-thread_local Workspace *g_ws = nullptr;
+// per thread and device: buffers cached by earlier calls on the device that
+// is current now (Ctx::init has selected it)
+thread_local Workspace *g_ws[MAX_DEVICES] = {};
 Workspace &ws() {
-  if (!g_ws) g_ws = new Workspace();
-  return *g_ws;
+  Workspace *&w = g_ws[ctx().device];
+  if (!w) w = new Workspace();
+  return *w;
 }
 
 void print_if(int verbose, const char *fmt, ...) {
@@ -231,9 +237,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
       h2d(t.r0.p, sg->r0.data(), ng);
       t.count = ng;
     } else {
-      std::vector<int> h(N);
-      for (ll i = 0; i < N; i++) h[i] = (int)i;
-      h2d(perm.p, h.data(), N);
+      iota_device(perm.p, N);
       t.reserve(1);
       ll s0 = 0, n0 = N;
       int p0 = P, r00 = 0;
@@ -272,9 +276,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     CK_LAUNCH();
     if (d_seq) {  // elements stay in input order inside their block
       DBuf<int> perm((size_t)N), first((size_t)nparts);
-      std::vector<int> h(N);
-      for (ll i = 0; i < N; i++) h[i] = (int)i;
-      h2d(perm.p, h.data(), N);
+      iota_device(perm.p, N);
       k_seq_from_order<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
       CK_LAUNCH();
       k_seq_write<<<grid_for(N, 256), 256, 0, st>>>(perm.p, d_part, N, first.p, d_seq);
@@ -611,19 +613,81 @@ extern "C" int parrsb_part_quality(double *q, const int *part, const long long *
   });
 }
 
+extern "C" int parrsb_dual_graph(long long *rowptr, int *col, unsigned char *weight,
+                                 long long *nnz, long long cap, const long long *vtx, int nel,
+                                 int nv) {
+  if (!nnz || nel < 0 || nv < 1 || nv > 8 || cap < 0) return PARRSB_ERR_ARGS;
+  if (nel > 0 && (!vtx || !rowptr)) return PARRSB_ERR_ARGS;
+  return guarded([&]() -> int {
+    ctx().init();
+    ll N = nel;
+    *nnz = 0;
+    if (N == 0) {
+      if (rowptr) rowptr[0] = 0;
+      return PARRSB_OK;
+    }
+    DBuf<long long> dv((size_t)N * nv);
+    h2d(dv.p, vtx, (size_t)N * nv);
+    std::vector<ll> rp;
+    std::vector<int> c;
+    std::vector<unsigned char> w;
+    dual_graph_device(dv.p, N, nv, rp, c, w);
+    *nnz = (long long)c.size();
+    memcpy(rowptr, rp.data(), (size_t)(N + 1) * sizeof(long long));
+    if (col && weight && (ll)c.size() <= cap) {
+      memcpy(col, c.data(), c.size() * sizeof(int));
+      memcpy(weight, w.data(), w.size());
+    }
+    ctx().stats.kernel_launches = ctx().kernel_launches;
+    return PARRSB_OK;
+  });
+}
+
+extern "C" int parrsb_components(int *ncomp, const long long *vtx, const int *group, int nel,
+                                 int nv, int ngroups) {
+  if (!ncomp || nel < 0 || nv < 1 || nv > 8 || ngroups < 1) return PARRSB_ERR_ARGS;
+  if (nel > 0 && (!vtx || !group)) return PARRSB_ERR_ARGS;
+  for (int e = 0; e < nel; e++)
+    if (group[e] >= ngroups) return PARRSB_ERR_ARGS;
+  return guarded([&]() -> int {
+    ctx().init();
+    ll N = nel;
+    std::vector<int> c(ngroups, 0);
+    if (N > 0) {
+      DBuf<long long> dv((size_t)N * nv);
+      DBuf<int> dg((size_t)N);
+      h2d(dv.p, vtx, (size_t)N * nv);
+      h2d(dg.p, group, (size_t)N);
+      components_device(dv.p, N, nv, dg.p, ngroups, c.data());
+    }
+    for (int g = 0; g < ngroups; g++) ncomp[g] = c[g];
+    ctx().stats.kernel_launches = ctx().kernel_launches;
+    return PARRSB_OK;
+  });
+}
+
 extern "C" void parrsb_gpu_finalize(void) {
-  if (g_ws) {
-    delete g_ws;
-    g_ws = nullptr;
+  // every device this thread used: free its workspace on its own stream,
+  // trim its pool and destroy the stream, with that device current
+  int cur = 0;
+  if (cudaGetDevice(&cur) != cudaSuccess) return;
+  for (int dev = 0; dev < MAX_DEVICES; dev++) {
+    if (!g_ws[dev] && !g_ctx.streams[dev]) continue;
+    if (cudaSetDevice(dev) != cudaSuccess) continue;
+    g_ctx.device = dev;
+    g_ctx.stream = g_ctx.streams[dev];
+    if (g_ws[dev]) {
+      delete g_ws[dev];
+      g_ws[dev] = nullptr;
+    }
+    if (g_ctx.stream) {
+      cudaStreamSynchronize(g_ctx.stream);
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+      cudaStreamDestroy(g_ctx.stream);
+      g_ctx.streams[dev] = nullptr;
+    }
   }
-  if (g_ctx.stream) {
-    cudaStreamSynchronize(g_ctx.stream);
-    int dev = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
-      cudaMemPoolTrimTo(pool, 0);
-    cudaStreamDestroy(g_ctx.stream);
-    g_ctx.stream = nullptr;
-  }
+  g_ctx.stream = nullptr;
+  cudaSetDevice(cur);
 }

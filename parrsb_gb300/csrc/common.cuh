@@ -84,8 +84,14 @@ struct DBuf {
   T *get() const { return p; }
 };
 
+// One per host thread.  Every call runs on the device that is current when
+// it starts: init() selects that device's stream (created on first use) and
+// workspace, so a thread may switch devices between calls.
+constexpr int MAX_DEVICES = 64;
 struct Ctx {
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // the current device's library stream
+  int device = 0;
+  cudaStream_t streams[MAX_DEVICES] = {};
   parrsb_stats stats;
   long long kernel_launches = 0;
   bool timing = false;  // time SpMV launches with events
@@ -152,6 +158,15 @@ inline void d2h(T *h, const T *d, size_t n) {
   if (n) CK(cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, ctx().stream));
 }
 inline void sync() { CK(cudaStreamSynchronize(ctx().stream)); }
+
+// cudaFuncSetAttribute acts on the current device only.  Raise `func`'s
+// dynamic shared-memory limit to at least `bytes` on the current device,
+// once per (kernel, device); thread-safe.
+cudaError_t smem_limit_on_device(const void *func, int bytes);
+template <typename K>
+inline void ensure_smem_limit(K *func, int bytes) {
+  CK(smem_limit_on_device(reinterpret_cast<const void *>(func), bytes));
+}
 
 inline unsigned grid_for(ll n, int threads) {
   ll g = (n + threads - 1) / threads;

@@ -963,7 +963,6 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   __shared__ float2 cs[LZ_TILE / 32 + 1];  // chunk pairs
   __shared__ ll soff[LZ_TILE / 32 + 2];
   __shared__ __align__(8) unsigned long long bars[SP_NST];
-  __shared__ int s_bad;
   const int t = blockIdx.x;
   const int g = tgrp[t];
   if (!gs[g].run && !force) return;
@@ -975,17 +974,24 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   const int nst = (nc + nw - 1) / nw;  // stages of nw slices
   for (int q = threadIdx.x; q <= nc; q += blockDim.x) soff[q] = slice_off[c0 + q];
   if (threadIdx.x == 0) {
-    s_bad = 0;
     for (int k = 0; k < SP_NST; k++) mbar_init(smem_u32addr(&bars[k]), 1);
     mbar_fence_init();
   }
   __syncthreads();
+  // Thread 0 issues the copies; a stage larger than its buffer is never
+  // copied (issue_bad).  `bad` is block-uniform (barrier-reduced): once a
+  // wait gives up or a stage is oversized, no further copy is issued, the
+  // block stops computing, drains the copies still in flight (bounded
+  // waits) and reports through err.
+  bool issue_bad = false;
+  int issued = 0;  // stages issued so far (thread 0)
   auto issue = [&](int j) {  // thread 0: stage j into buffer j % SP_NST
     const int q0 = j * nw, q1 = min(q0 + nw, nc);
     const u32 bytes = (u32)((soff[q1] - soff[q0]) * 4);
     const u32 bar = smem_u32addr(&bars[j % SP_NST]);
+    issued = j + 1;
     if (bytes > (u32)stage_bytes) {  // never copy past the stage buffer
-      s_bad = 1;
+      issue_bad = true;
       mbar_arrive(bar);
     } else if (bytes == 0) {
       mbar_arrive(bar);
@@ -997,11 +1003,15 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   };
   if (threadIdx.x == 0)
     for (int j = 0; j < SP_NST && j < nst; j++) issue(j);
-  for (int j = 0; j < nst; j++) {
+  bool bad = false;
+  int j = 0;
+  for (; j < nst; j++) {
     const int buf = j % SP_NST;
-    if (!mbar_wait(smem_u32addr(&bars[buf]), (u32)((j / SP_NST) & 1))) s_bad = 1;
+    const bool ok = mbar_wait(smem_u32addr(&bars[buf]), (u32)((j / SP_NST) & 1));
+    bad = __syncthreads_or(!ok || issue_bad) != 0;
+    if (bad) break;
     const int q = j * nw + warp;
-    if (q < nc && !s_bad) {
+    if (q < nc) {
       const ll sl = c0 + q;
       const ll i = sl * 32 + lane;
       const bool valid = i >= b && i < e;
@@ -1040,10 +1050,18 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     __syncthreads();  // buffer j % SP_NST is free again
     if (threadIdx.x == 0 && j + SP_NST < nst) issue(j + SP_NST);
   }
+  if (bad) {
+    // stages j .. issued - 1 may still be in flight (stage j's wait gave up
+    // or it was oversized): wait for each once more, bounded, so that no
+    // copy is left writing into this block's shared memory if it can end
+    if (threadIdx.x == 0)
+      for (int k = j; k < issued; k++) mbar_wait(smem_u32addr(&bars[k % SP_NST]), (u32)((k / SP_NST) & 1));
+    __syncthreads();
+  }
   if (threadIdx.x < 32) {
-    const double v0 = tile_total_pair(cs, nc);
+    const double v0 = bad ? 0.0 : tile_total_pair(cs, nc);
     if (threadIdx.x == 0) {
-      if (s_bad) atomicExch(err, 1);
+      if (bad) atomicExch(err, 1);
       part[t] = v0;
     }
   }
@@ -1618,6 +1636,9 @@ struct Lanczos {
   // a result.  Decisions are cached per (tiles, groups, rows) for the thread.
   void autotune(const Level &lv) {
     // PARRSB_GPU_SPMV: 0 = k_spmv only, 1 = k_spmv_tma only, unset = time both
+    // per device (a later call may run on another device), before the cached
+    // decision is used
+    ensure_smem_limit(k_spmv_tma, 200 * 1024);
     const char *force_env = getenv("PARRSB_GPU_SPMV");
     const int force_kind = force_env ? atoi(force_env) : -1;
     static thread_local std::vector<std::pair<std::array<ll, 5>, int>> cache;
@@ -1632,12 +1653,6 @@ struct Lanczos {
         return;
       }
     cudaStream_t st = ctx().stream;
-    static bool attr_set = false;
-    if (!attr_set) {
-      CK(cudaFuncSetAttribute(k_spmv_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              200 * 1024));
-      attr_set = true;
-    }
     std::vector<std::pair<int, int>> cand;
     for (int th : {128, 256, 512}) {
       if (force_th && th != force_th) continue;
@@ -2073,9 +2088,6 @@ void build_level(const Graph &g, const int *perm, const int *inv, const int *grp
   CK_LAUNCH();
   // restricted nnz of active rows (for the algorithmic byte count)
   DBuf<ll> rl64((size_t)N);
-  // reuse scan: sum of row lengths
-  std::vector<int> hr;  // small N only would be cheap; use a device reduction instead
-  (void)hr;
   ll nnz = exclusive_scan_int_to_ll(rowlen.p, rl64.p, N);
   lv.nnz = nnz;
   DBuf<int> mw(1);
@@ -2084,6 +2096,61 @@ void build_level(const Graph &g, const int *perm, const int *inv, const int *grp
   CK_LAUNCH();
   d2h(&lv.max_w, mw.p, 1);
   sync();
+}
+
+// Number of vertex-connected components of every half (get_components_v2,
+// src/components.c:160-328, count only): min-label hooking plus pointer
+// jumping on the level graph restricted to each half.  half[i] is the half
+// id of position i (-1: none); hstart[h] is a position inside half h (its
+// first one).  Two one-edge hooking rounds join most of a half into one
+// tree; full rounds then visit only the rows outside the tree of hstart[h]
+// (PARRSB_GPU_CC_FULL=1: every row every round).  Returns the counts by id.
+std::vector<int> count_components_level(const Level &lv, const int *half, ll N,
+                                        const std::vector<ll> &hstart) {
+  cudaStream_t st = ctx().stream;
+  const int nh = (int)hstart.size();
+  std::vector<int> hc(nh, 0);
+  if (nh == 0 || N == 0) return hc;
+  DBuf<int> lab((size_t)N), changed(1), cnt((size_t)nh);
+  k_cc_init<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
+  CK_LAUNCH();
+  const bool full = env_flag("PARRSB_GPU_CC_FULL");
+  DBuf<int> giant((size_t)nh);
+  if (!full) {
+    for (int r = 0; r < 2; r++) {
+      k_cc_sample<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, half,
+                                                    N, r, lab.p);
+      CK_LAUNCH();
+      k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
+      CK_LAUNCH();
+    }
+    DBuf<ll> hs((size_t)nh);
+    h2d(hs.p, hstart.data(), nh);
+    k_cc_giant<<<grid_for(nh, 256), 256, 0, st>>>(hs.p, nh, lab.p, giant.p);
+    CK_LAUNCH();
+  }
+  for (int round = 0; round < 100000; round++) {
+    CK(cudaMemsetAsync(changed.p, 0, sizeof(int), st));
+    if (full)
+      k_cc_hook<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, half, N,
+                                                  lab.p, changed.p);
+    else
+      k_cc_hook_rest<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
+                                                       half, giant.p, N, lab.p, changed.p);
+    CK_LAUNCH();
+    k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
+    CK_LAUNCH();
+    int h = 0;
+    d2h(&h, changed.p, 1);
+    sync();
+    if (!h) break;
+  }
+  CK(cudaMemsetAsync(cnt.p, 0, (size_t)nh * sizeof(int), st));
+  k_cc_count<<<grid_for(N, 256), 256, 0, st>>>(lab.p, half, N, cnt.p);
+  CK_LAUNCH();
+  d2h(hc.data(), cnt.p, nh);
+  sync();
+  return hc;
 }
 
 template <typename VT>
@@ -2190,9 +2257,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     for (size_t g = 0; g < sg->start.size(); g++)
       groups.push_back({sg->start[g], sg->n[g], sg->p[g], sg->r0[g]});
   } else {
-    std::vector<int> h(N);
-    for (ll i = 0; i < N; i++) h[i] = (int)i;
-    h2d(perm.p, h.data(), N);
+    iota_device(perm.p, N);
     groups.push_back({0, N, P, 0});
   }
   int ncuts = 0;
@@ -2317,51 +2382,9 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     // ---- connected components of each half (src/rsb.c:319-327)
     if (o.find_comps) {
       StageTimer tm(PARRSB_STAGE_COMPONENTS);
-      DBuf<int> lab((size_t)N), changed(1), cnt((size_t)2 * na);
-      k_cc_init<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
-      CK_LAUNCH();
-      // PARRSB_GPU_CC_FULL=1: every round over every row (no sampling)
-      const bool full = env_flag("PARRSB_GPU_CC_FULL");
-      const int nh = 2 * na;
-      DBuf<int> giant((size_t)nh);
-      if (!full) {
-        for (int r = 0; r < 2; r++) {
-          k_cc_sample<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
-                                                        half.p, N, r, lab.p);
-          CK_LAUNCH();
-          k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
-          CK_LAUNCH();
-        }
-        std::vector<ll> hs_by_id(nh, 0);
-        for (size_t q = 0; q < hid.size(); q++) hs_by_id[hid[q]] = hst[q];
-        DBuf<ll> hs((size_t)nh);
-        h2d(hs.p, hs_by_id.data(), nh);
-        k_cc_giant<<<grid_for(nh, 256), 256, 0, st>>>(hs.p, nh, lab.p, giant.p);
-        CK_LAUNCH();
-      }
-      for (int round = 0; round < 100000; round++) {
-        CK(cudaMemsetAsync(changed.p, 0, sizeof(int), st));
-        if (full)
-          k_cc_hook<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p,
-                                                      half.p, N, lab.p, changed.p);
-        else
-          k_cc_hook_rest<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p,
-                                                           lv.slice_w.p, half.p, giant.p, N,
-                                                           lab.p, changed.p);
-        CK_LAUNCH();
-        k_cc_compress<<<grid_for(N, 256), 256, 0, st>>>(lab.p, N);
-        CK_LAUNCH();
-        int hc = 0;
-        d2h(&hc, changed.p, 1);
-        sync();
-        if (!hc) break;
-      }
-      CK(cudaMemsetAsync(cnt.p, 0, (size_t)2 * na * sizeof(int), st));
-      k_cc_count<<<grid_for(N, 256), 256, 0, st>>>(lab.p, half.p, N, cnt.p);
-      CK_LAUNCH();
-      std::vector<int> hc(2 * na);
-      d2h(hc.data(), cnt.p, 2 * na);
-      sync();
+      std::vector<ll> hs_by_id(2 * na, 0);
+      for (size_t q = 0; q < hid.size(); q++) hs_by_id[hid[q]] = hst[q];
+      std::vector<int> hc = count_components_level(lv, half.p, N, hs_by_id);
       for (int v : hc) S.max_components = std::max(S.max_components, v);
     }
     // ---- balance (src/rsb.c:118-229)
@@ -2619,6 +2642,81 @@ void fiedler_groups_device(const long long *d_vtx, ll N, int nv, const int *d_gr
     fiedler_groups_impl<float>(d_vtx, N, nv, d_group_of, ngroups, o, d_f, iters, resid);
   else
     fiedler_groups_impl<double>(d_vtx, N, nv, d_group_of, ngroups, o, d_f, iters, resid);
+}
+
+// keys for ordering elements by group; elements without a group (< 0) go last
+__global__ void k_group_keys_opt(const int *__restrict__ group_of, ll N, int ngroups,
+                                 u64 *__restrict__ keys, int *__restrict__ vals,
+                                 int *__restrict__ cnt) {
+  ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= N) return;
+  int g = group_of[e];
+  keys[e] = g >= 0 ? (u64)(unsigned)g : (u64)(unsigned)ngroups;
+  vals[e] = (int)e;
+  if (g >= 0) atomicAdd(&cnt[g], 1);
+}
+
+__global__ void k_iota(int *__restrict__ a, ll N) {
+  ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) a[i] = (int)i;
+}
+
+void iota_device(int *d, ll N) {
+  if (N <= 0) return;
+  k_iota<<<grid_for(N, 256), 256, 0, ctx().stream>>>(d, N);
+  CK_LAUNCH();
+}
+
+void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_of, int ngroups,
+                       int *counts) {
+  cudaStream_t st = ctx().stream;
+  for (int g = 0; g < ngroups; g++) counts[g] = 0;
+  if (N == 0) return;
+  SortWs sws;
+  Graph G;
+  build_dual_graph(d_vtx, N, nv, G, sws);
+  if (N >= (1ll << 28))
+    throw ArgError{PARRSB_ERR_UNSUPPORTED, "more than 2^28 elements"};
+  DBuf<u64> keys((size_t)N);
+  DBuf<int> perm((size_t)N), cnt((size_t)ngroups), inv((size_t)N), grp((size_t)N);
+  CK(cudaMemsetAsync(cnt.p, 0, (size_t)ngroups * sizeof(int), st));
+  k_group_keys_opt<<<grid_for(N, 256), 256, 0, st>>>(d_group_of, N, ngroups, keys.p, perm.p,
+                                                     cnt.p);
+  CK_LAUNCH();
+  seg_sort_pairs(keys, perm, N, nullptr, 1, sws);
+  std::vector<int> hc(ngroups);
+  d2h(hc.data(), cnt.p, ngroups);
+  sync();
+  std::vector<ll> st_, n_, hstart(ngroups, 0);
+  std::vector<int> id_;
+  ll pos = 0;
+  for (int g = 0; g < ngroups; g++) {
+    st_.push_back(pos), n_.push_back(hc[g]), id_.push_back(g);
+    hstart[g] = hc[g] ? pos : 0;  // any valid row for an empty group (never consulted)
+    pos += hc[g];
+  }
+  CK(cudaMemsetAsync(grp.p, 0xff, (size_t)N * sizeof(int), st));  // no group: -1
+  fill_groups(st_, n_, id_, grp.p, N);
+  k_inv_perm<<<grid_for(N, 256), 256, 0, st>>>(perm.p, N, inv.p);
+  CK_LAUNCH();
+  Level lv;
+  build_level(G, perm.p, inv.p, grp.p, N, lv);
+  std::vector<int> c = count_components_level(lv, grp.p, N, hstart);
+  for (int g = 0; g < ngroups; g++) counts[g] = hc[g] ? c[g] : 0;
+}
+
+void dual_graph_device(const long long *d_vtx, ll N, int nv, std::vector<ll> &rowptr,
+                       std::vector<int> &col, std::vector<unsigned char> &w) {
+  SortWs sws;
+  Graph G;
+  build_dual_graph(d_vtx, N, nv, G, sws);
+  rowptr.assign((size_t)N + 1, 0);
+  col.assign((size_t)G.nnz, 0);
+  w.assign((size_t)G.nnz, 0);
+  d2h(rowptr.data(), G.rowptr.p, (size_t)N + 1);
+  d2h(col.data(), G.col.p, (size_t)G.nnz);
+  d2h(w.data(), G.w.p, (size_t)G.nnz);
+  sync();
 }
 
 void rsb_device(const long long *d_vtx, const double *cent, ll N, int nv, int P,

@@ -58,6 +58,19 @@ void fiedler_groups_device(const long long *d_vtx, ll N, int nv,
                            const RsbOpts &o, double *d_f, long long *iters,
                            double *resid);
 
+// Vertex-connected components of each group (group_of[e] < 0: no group);
+// counts (host, ngroups) receives the number per group.
+void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_of,
+                       int ngroups, int *counts);
+
+// The element dual graph as built for RSB (rows in element order, each row's
+// columns in first-occurrence order), copied to the host.
+void dual_graph_device(const long long *d_vtx, ll N, int nv, std::vector<ll> &rowptr,
+                       std::vector<int> &col, std::vector<unsigned char> &w);
+
+// d[i] = i for i < N on the library stream.
+void iota_device(int *d, ll N);
+
 // Quality of a partition (see parrsb_part_quality).
 void part_quality_device(const long long *d_vtx, const int *d_part, ll N,
                          int nv, int nparts, double *q);

@@ -291,12 +291,7 @@ void seg_sort_pairs(DBuf<u64> &keys, DBuf<int> &vals, ll n,
     passes[npasses].shift = b >= nkey ? 8 * (b - nkey) : 8 * b;
     npasses++;
   }
-  static bool scatter_attr = false;  // staging buffers exceed the 48 KB default
-  if (!scatter_attr) {
-    CK(cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                            (int)SCATTER_SMEM));
-    scatter_attr = true;
-  }
+  ensure_smem_limit(k_scatter, (int)SCATTER_SMEM);  // staging exceeds the 48 KB default
   for (int q = 0; q < npasses; q++) {
     const PassDesc &pd = passes[q];
     k_tile_hist<<<ntiles, SORT_THREADS, 0, st>>>(keys.p, vals.p, n, seg_of_val,

@@ -1,4 +1,8 @@
 // util.cu -- three-phase exclusive scan and segment-table helpers.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "util.cuh"
 
 namespace prsb {
@@ -121,6 +125,21 @@ void fill_seg_of_pos(const SegTable &t, int *seg_of_pos, ll N) {
   k_fill_seg_of_pos<<<grid_for(N, 256), 256, 0, ctx().stream>>>(t.start.p, t.count,
                                                                  seg_of_pos, N);
   CK_LAUNCH();
+}
+
+cudaError_t smem_limit_on_device(const void *func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> done;  // (kernel, device) -> bytes set
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(func, dev);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done[key] = bytes;
+  return e;
 }
 
 }  // namespace prsb

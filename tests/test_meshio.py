@@ -9,7 +9,10 @@ import pytest
 import parrsb_gb300 as P
 from parrsb_gb300 import meshgen
 
-ETHIER = "/root/reference/examples/ethier"
+# stem of the reference's examples/ethier mesh (only where a reference tree
+# is available; the committed fixture stands in for it elsewhere)
+ETHIER = os.environ.get("PARRSB_ETHIER", "")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ethier.npz")
 
 
 def test_re2_roundtrip(tmp_path, lib):
@@ -61,10 +64,12 @@ def test_missing_file_is_an_error(tmp_path, lib):
         P.read_mesh(str(tmp_path / "nope"), read=1)
 
 
-@pytest.mark.skipif(not os.path.exists(ETHIER + ".re2"), reason="reference tree absent")
+@pytest.mark.skipif(not os.path.exists(ETHIER + ".re2"),
+                    reason="set PARRSB_ETHIER to the stem of the reference's examples/ethier")
 def test_ethier_mesh_through_gencon_oracle(oracle, lib):
     """examples/ethier.re2 (32 hex elements, used by the reference's CI):
-    read, number with the oracle's gencon, check the connectivity."""
+    read, number with the oracle's gencon, check the connectivity, and
+    check that the committed fixture was made from this file."""
     m = P.read_mesh(ETHIER, read=1)
     coord = m["coord"]
     assert coord.shape == (32, 8, 3)
@@ -74,3 +79,21 @@ def test_ethier_mesh_through_gencon_oracle(oracle, lib):
     rch, idsh, _, _ = oracle.conn_mesh(coord, 3, 0.2, heapsort=True)
     assert rch == 0
     np.testing.assert_array_equal(ids, idsh)
+    g = np.load(GOLDEN)
+    np.testing.assert_array_equal(g["coord"], coord)
+
+
+def test_ethier_fixture_pins_the_oracle(oracle):
+    """The committed ethier fixture (tests/golden/make_ethier.py): the
+    oracle's gencon ids, heapsort mode included, and its RCB / RSB parts."""
+    g = np.load(GOLDEN)
+    rc, ids, _, nseg = oracle.conn_mesh(g["coord"], 3, 0.2)
+    assert rc == 0 and nseg == int(g["nseg"])
+    np.testing.assert_array_equal(ids, g["vtx"])
+    rch, idsh, _, _ = oracle.conn_mesh(g["coord"], 3, 0.2, heapsort=True)
+    assert rch == 0
+    np.testing.assert_array_equal(idsh, g["vtx"])
+    rc1, rcb, _, _, _ = oracle.part_mesh(g["vtx"], g["coord"], 4, partitioner=1)
+    np.testing.assert_array_equal(rcb, g["rcb4"])
+    rc0, rsb, _, _, _ = oracle.part_mesh(g["vtx"], g["coord"], 4, partitioner=0)
+    np.testing.assert_array_equal(rsb, g["rsb4"])
