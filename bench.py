@@ -31,8 +31,15 @@ sys.path.insert(0, ROOT)
 METRIC = "RSB s, 8M hex→1024 parts: warm+batched vs plain GPU, cut±1%, tol 1e-5"
 SHAPE = (256, 256, 128)
 NPARTS = 1024
-SAMPLE_SHAPE = (80, 80, 40)   # CPU sample: 8000 elements per part, same aspect
-SAMPLE_PARTS = 32
+
+
+def workload_config(shape, nparts):
+    """The workload, identical in both arms' lines."""
+    return {"workload": f"rsb_hex_box_{'x'.join(map(str, shape))}_to_{nparts}_parts",
+            "elements": shape[0] * shape[1] * shape[2], "nparts": nparts, "rsb_tol": 1e-5,
+            "rsb_max_iter": 50, "rsb_max_passes": 50, "rsb_pre": "rcb",
+            "mesh": "jittered hex box on [0,1]^3, jitter 0.1 h, seed 0",
+            "l2": "inputs (2.1 GB mesh) larger than L2"}
 
 
 def parse():
@@ -137,16 +144,14 @@ def load_traffic():
     return None
 
 
-def cpu_sample_seconds(shape, nparts):
-    """Run the oracle's RSB once on the sample mesh; returns wall seconds."""
-    from parrsb_gb300 import meshgen
-    from oracle import oracle as O
-    vtx, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=0)
-    t = time.perf_counter()
-    rc, part, _, info, _ = O.part_mesh(vtx, xyz, nparts, partitioner=0)
-    dt = time.perf_counter() - t
-    assert rc == 0
-    return dt, info.total_iters
+def load_fixture(name):
+    """Oracle RSB of the workload (tests/golden/make_rsb_fixtures.py)."""
+    path = os.path.join(ROOT, "tests", "golden", f"rsb_{name}.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
 
 
 def _levels(p):
@@ -156,47 +161,108 @@ def _levels(p):
     return n
 
 
-def scale_to_workload(sample_seconds, shape, nparts):
-    """Element-levels of the full workload over those of the sample."""
-    full = SHAPE[0] * SHAPE[1] * SHAPE[2] * _levels(NPARTS)
-    samp = shape[0] * shape[1] * shape[2] * _levels(nparts)
-    return sample_seconds * full / samp
+def workload_name(shape, nparts):
+    return f"hex_box_{'x'.join(map(str, shape))}_to_{nparts}"
+
+
+def cpu_level0_seconds(vtx, xyz, nparts, threads):
+    """CPU baseline sample: the oracle's first bisection (level 0: RCB
+    pre-partition, dual graph, Lanczos, sort, components) of the workload
+    itself on `threads` host threads.  Returns (seconds, rows x steps)."""
+    from oracle import oracle as O
+    O.build()
+    O.threads(threads)
+    lv = O.RsbLevels(vtx, xyz, nparts)
+    t = time.perf_counter()
+    lv.level()
+    return time.perf_counter() - t, lv.info.row_iters
 
 
 def run_reference(args):
+    """The reference arm: the oracle (CPU restatement of the reference's
+    RSB) on the workload itself, on all host threads.  One step is one RSB
+    level of the real 8M -> 1024 partition (a bounded sample of the
+    workload): steps run the levels in order, one partition after another
+    (step s runs level s mod L of partition s div L, its input the previous
+    step's output), warm-up steps first.  value = the sum over the L levels
+    of each level's median timed time: seconds per whole partition, every
+    level measured on its real input.  Levels that no timed step reached
+    are run once after the timed region and enter with that time."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import multiprocessing as mp
     from oracle import oracle as O
+    from parrsb_gb300 import meshgen
     O.build()
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    times = []
-    with ctx.Pool(cores) as pool:
-        for step in range(args.warmup + args.steps):
-            t = time.perf_counter()
-            res = pool.starmap(cpu_sample_seconds, [(SAMPLE_SHAPE, SAMPLE_PARTS)] * cores)
-            wall = time.perf_counter() - t
-            if step >= args.warmup:
-                times.append(wall)
-    # `cores` samples in `wall` seconds: throughput of the whole host
-    per_sample = statistics.median(times) / cores
-    est = scale_to_workload(per_sample, SAMPLE_SHAPE, SAMPLE_PARTS)
+    O.threads(cores)
+    shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else SHAPE
+    nparts = args.nparts or NPARTS
+    vtx, xyz = meshgen.box_hex(*shape, jitter=0.1, seed=0)
+    lv = O.RsbLevels(vtx, xyz, nparts)
+    ncuts = lv.ncuts
+    fresh = lv.state()
+    timed = {L: [] for L in range(ncuts)}
+    step_t = []
+    quality = None
+
+    def one_level(s):
+        nonlocal quality
+        L = s % ncuts
+        if L == 0:
+            lv.restore(fresh)
+            lv.info = O.RsbInfo()
+        t = time.perf_counter()
+        lv.level()
+        dt = time.perf_counter() - t
+        if L == ncuts - 1 and quality is None:  # first complete partition
+            part = lv.part()
+            q = O.part_quality(part, vtx, nparts)
+            quality = {"weighted_cut": q[0], "imbalance": q[5],
+                       "lanczos_steps": int(lv.info.total_iters),
+                       "max_fiedler_resid": lv.info.max_resid}
+        return L, dt
+
+    s = 0
+    for _ in range(args.warmup):
+        one_level(s)
+        s += 1
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        L, dt = one_level(s)
+        s += 1
+        timed[L].append(dt)
+        step_t.append(dt)
+    timed_wall = time.perf_counter() - t_all
+    untimed = {}
+    while any(not timed[L] for L in range(ncuts)) or quality is None:
+        L, dt = one_level(s)
+        s += 1
+        if not timed[L]:
+            untimed[L] = dt
+    per_level = [statistics.median(timed[L]) if timed[L] else untimed[L] for L in range(ncuts)]
+    value = sum(per_level)
+    fx = load_fixture(workload_name(shape, nparts))
+    quality["equals_fixture"] = bool(fx is not None
+                                     and quality["weighted_cut"] == fx["weighted_cut"]
+                                     and quality["lanczos_steps"] == fx["lanczos_steps"])
     out = {
-        "impl": "reference", "metric": METRIC, "value": est, "unit": "s",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": statistics.median(times) * 1e3, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "rsb_hex_box_256x256x128_to_1024_parts",
-                   "elements": SHAPE[0] * SHAPE[1] * SHAPE[2], "nparts": NPARTS,
-                   "l2": "inputs larger than L2"},
-        "cpu_baseline": {"value": est, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": (f"{cores} concurrent oracle RSB runs of a "
-                                    f"{'x'.join(map(str, SAMPLE_SHAPE))} box to "
-                                    f"{SAMPLE_PARTS} parts (8000 elements per part), "
-                                    "time scaled by elements x bisection levels")},
-        "e2e": {"value": est, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "ms_per_step": statistics.mean(step_t) * 1e3 if step_t else None,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": workload_config(shape, nparts),
+        "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": (f"oracle RSB of the workload itself on {cores} host threads; "
+                                    f"one step = one of its {ncuts} levels on that level's real "
+                                    "input, levels in order, partition after partition; value = "
+                                    "sum of the levels' median step times"
+                                    + (f" ({len(untimed)} levels untimed: timed once after the "
+                                       "timed region)" if untimed else ""))},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "timed_region_s": timed_wall,
+        "level_s": [round(x, 3) for x in per_level],
+        "quality": quality,
     }
     print(json.dumps(out))
 
@@ -421,14 +487,23 @@ def main():
         tr_val = tr_val * per_launch_bytes if tr_val else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import oracle as O
-        O.build()
-        dt, _ = cpu_sample_seconds(SAMPLE_SHAPE, SAMPLE_PARTS)
-        cpu = {"value": scale_to_workload(dt, SAMPLE_SHAPE, SAMPLE_PARTS), "unit": "s",
-               "cores": 1, "kind": "port",
-               "sample": (f"oracle RSB of a {'x'.join(map(str, SAMPLE_SHAPE))} box to "
-                          f"{SAMPLE_PARTS} parts (8000 elements per part) took {dt:.1f} s; "
-                          "scaled by elements x bisection levels")}
+        # the first bisection of this workload on all host threads, scaled to
+        # the whole partition by the oracle's own rows x Lanczos steps per
+        # level (committed fixture of the full oracle run)
+        threads = os.cpu_count() or 1
+        dt, rows0 = cpu_level0_seconds(vtx, xyz, nparts, threads)
+        fx = load_fixture(workload_name(shape, nparts))
+        if fx and fx["levels"] and fx["levels"][0]["row_steps"] == rows0:
+            scale = fx["row_steps"] / rows0
+            how = (f"level 0 of this workload took {dt:.2f} s; scaled by the oracle's rows x "
+                   f"Lanczos steps of all levels over level 0's ({scale:.2f}, fixture "
+                   f"tests/golden/rsb_{workload_name(shape, nparts)}.json)")
+        else:
+            scale = float(_levels(nparts))
+            how = (f"level 0 of this workload took {dt:.2f} s; scaled by the number of "
+                   f"levels ({scale:.0f}); no matching fixture")
+        cpu = {"value": dt * scale, "unit": "s", "cores": threads, "kind": "port",
+               "sample": how}
     h2d = vtx.nbytes + xyz.nbytes
     out = {
         "metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world,
@@ -436,11 +511,8 @@ def main():
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if os.environ.get("PARRSB_GPU_FP32", "0") == "1" else "f64",
         "data": "synthetic",
-        "config": {"workload": f"rsb_hex_box_{'x'.join(map(str, shape))}_to_{nparts}_parts",
-                   "elements": nel, "nparts": nparts, "rsb_tol": 1e-5,
-                   "rsb_max_iter": 50, "rsb_max_passes": 50, "rsb_pre": "rcb",
-                   "batched": "all groups of a level per launch, one CUDA graph per pass",
-                   "l2": "inputs (2.1 GB mesh) larger than L2",
+        "config": workload_config(shape, nparts),
+        "method": {"batched": "all groups of a level per launch, one CUDA graph per pass",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(part.nbytes), "last_call": e2e_stages},

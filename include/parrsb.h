@@ -164,6 +164,11 @@ typedef struct {
   double lanczos_ms[6];       /* timing mode: p update, r update, eigensolve,
                                  Ritz vector, pass set-up, host per pass */
   long long lanczos_passes;   /* graph launches (Lanczos restarts of a level) */
+  long long warm_tried;       /* groups whose learned warm start was judged */
+  long long warm_used;        /* of those, groups that started from it */
+  double warm_ms;             /* warm-start network inference (all levels) */
+  double start_resid_fallback;/* geometric mean of the judged groups' start */
+  double start_resid_warm;    /*   residuals: fallback and learned starts */
 } parrsb_stats;
 
 enum {
@@ -226,6 +231,57 @@ PARRSB_API int parrsb_dual_graph(long long *rowptr, int *col, unsigned char *wei
  * component check of each bisection.  Host arrays. */
 PARRSB_API int parrsb_components(int *ncomp, const long long *vtx, const int *group, int nel,
                                  int nv, int ngroups);
+
+/* ------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference, which starts every
+ * Lanczos run from a step vector in the current element order,
+ * src/fiedler.c:574-578).  A three-layer message-passing network (width 64,
+ * BF16 weights and activations, FP32 accumulation on the tensor cores)
+ * predicts each group's Fiedler vector from its elements' centroids (in the
+ * group's principal frame) and weighted degrees, over the graph Lanczos
+ * itself multiplies by.  With PARRSB_GPU_WARM=1, RSB judges the prediction
+ * of every group of at least PARRSB_GPU_WARM_MIN elements against the
+ * fallback start (PARRSB_GPU_START: 0 the reference's step vector, 1 a
+ * seeded random vector) by their FP64 eigen-residuals ||L f - rho f|| /
+ * ||f|| and starts Lanczos from the better one; Lanczos then iterates to
+ * rsb_tol as usual.  The network is installed per device with
+ * parrsb_warm_install, or read from the raw FP32 file named by
+ * PARRSB_GPU_WARM_WEIGHTS.  The batch entry points train it on the GPU with
+ * the same kernels (device pointers on the current device).
+ * ---------------------------------------------------------------------- */
+#define PARRSB_WARM_NPARAM 17665
+
+/* Install the network's parameters (host FP32, PARRSB_WARM_NPARAM values:
+ * W1[16][64], b1[64], W2[128][64], b2[64], W3[128][64], b3[64], wo[64], bo)
+ * for the current device. */
+PARRSB_API int parrsb_warm_install(const float *params);
+
+typedef struct parrsb_warm_batch parrsb_warm_batch;
+
+/* A training batch: the elements of each group (d_group[e] in [0, ngroups))
+ * form one mesh; its graph and input features are built once.  d_vtx:
+ * nel * nv vertex ids, d_xyz: nel * nv * ndim corner coordinates. */
+PARRSB_API int parrsb_warm_batch_create(parrsb_warm_batch **batch, const long long *d_vtx,
+                                        const double *d_xyz, const int *d_group, int nel,
+                                        int nv, int ngroups);
+PARRSB_API int parrsb_warm_batch_destroy(parrsb_warm_batch *batch);
+
+/* The batch's input features, nel x 8 FP32 in element order. */
+PARRSB_API int parrsb_warm_batch_features(parrsb_warm_batch *batch, float *d_feat);
+
+/* Forward pass with parameters d_params (device FP32); d_pred (optional):
+ * the prediction per element.  With d_label (per element, FP64): the mean
+ * over groups of the sign-invariant loss 1 - cos^2(prediction, label) (both
+ * centred) in *loss and, if d_grad is not NULL, its gradient with respect to
+ * every parameter (device FP32, PARRSB_WARM_NPARAM values). */
+PARRSB_API int parrsb_warm_batch_step(parrsb_warm_batch *batch, const float *d_params,
+                                      const double *d_label, float *d_grad, float *d_pred,
+                                      double *loss);
+
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8; step >= 1) on n device
+ * parameters with moment buffers d_m, d_v. */
+PARRSB_API int parrsb_warm_adam(float *d_params, float *d_m, float *d_v, const float *d_grad,
+                                int n, int step, float lr);
 
 /* Release the device workspace cached by earlier calls on this thread. */
 PARRSB_API void parrsb_gpu_finalize(void);

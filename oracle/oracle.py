@@ -26,9 +26,12 @@ def build(force=False):
     newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
-    cmd = ["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", LIB + ".tmp", SRC, "-lm"]
-    subprocess.run(cmd, check=True)
+    base = ["gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared",
+            "-o", LIB + ".tmp", SRC, "-lm"]
+    # OpenMP when the compiler has it (host threads for large meshes; the
+    # results do not depend on the thread count), plain otherwise
+    if subprocess.run(base + ["-fopenmp"], capture_output=True).returncode != 0:
+        subprocess.run(base, check=True)
     os.replace(LIB + ".tmp", LIB)
     return LIB
 
@@ -36,7 +39,8 @@ def build(force=False):
 class RsbInfo(ctypes.Structure):
     _fields_ = [("total_iters", ctypes.c_longlong), ("nbisect", ctypes.c_int),
                 ("unconverged", ctypes.c_int), ("max_components", ctypes.c_int),
-                ("max_resid", ctypes.c_double), ("levels", ctypes.c_int)]
+                ("max_resid", ctypes.c_double), ("levels", ctypes.c_int),
+                ("row_iters", ctypes.c_longlong)]
 
 
 def lib():
@@ -67,6 +71,12 @@ def lib():
                                           ctypes.c_int]
         L.oracle_fiedler.argtypes = [P, P, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, ctypes.c_double]
+        L.oracle_rsb_level.argtypes = [P, P, ctypes.c_int, P, P, P, ctypes.c_int,
+                                       ctypes.c_int, ctypes.POINTER(ParrsbOptions),
+                                       ctypes.POINTER(RsbInfo)]
+        L.oracle_rsb_level.restype = ctypes.c_int
+        L.oracle_threads.argtypes = [ctypes.c_int]
+        L.oracle_threads.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -89,6 +99,50 @@ def part_mesh(vtx, xyz, nparts, want_order=False, **opts):
     rc = lib().oracle_part_mesh(_p(part), _p(order), _p(vtx), _p(xyz), nel, nv,
                                 ctypes.byref(o), nparts, ctypes.byref(info))
     return rc, part, order, info, o
+
+
+def threads(n=0):
+    """Host threads of the oracle (n > 0 sets them); returns the count."""
+    return lib().oracle_threads(int(n))
+
+
+class RsbLevels:
+    """RSB of the oracle one level at a time (oracle_rsb_level), for timing
+    the levels of a large run separately.  state() / restore() copy the
+    element order and segment table at a level boundary."""
+
+    def __init__(self, vtx, xyz, nparts, **opts):
+        self.vtx = np.ascontiguousarray(vtx, np.int64)
+        self.nel, self.nv = self.vtx.shape
+        opts.setdefault("verbose_level", 0)
+        self.opts = ParrsbOptions.make(partitioner=0, **opts)
+        self.cent = centroids(xyz, self.nv)
+        self.P = min(nparts, self.nel)
+        self.a = np.arange(self.nel, dtype=np.int32)
+        self.segs = np.array([[0, self.nel, self.P, 0]], np.int64)
+        self.info = RsbInfo()
+        self.ncuts = 0
+        while (1 << self.ncuts) < self.P:
+            self.ncuts += 1
+
+    def state(self):
+        return self.a.copy(), self.segs.copy()
+
+    def restore(self, st):
+        self.a, self.segs = st[0].copy(), st[1].copy()
+
+    def level(self):
+        out = np.zeros((2 * len(self.segs), 4), np.int64)
+        n = lib().oracle_rsb_level(_p(self.a), _p(self.segs), len(self.segs), _p(out),
+                                   _p(self.vtx), _p(self.cent), self.nel, self.nv,
+                                   ctypes.byref(self.opts), ctypes.byref(self.info))
+        self.segs = out[:n].copy()
+
+    def part(self):
+        part = np.full(self.nel, -1, np.int32)
+        for s0, n, p, r0 in self.segs:
+            part[self.a[s0:s0 + n]] = r0
+        return part
 
 
 def conn_mesh(coord, ndim, tol=0.2, heapsort=False, periodic=None):

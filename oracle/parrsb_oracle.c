@@ -22,9 +22,70 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 typedef long long ll;
 
 #define SCALAR_TOL 1e-12 /* src/parrsb-impl.h:20 */
+
+/* ------------------------------------------------------------------------ */
+/* Host threads (OpenMP when the oracle is built with it).  The reference    */
+/* runs one MPI rank per part; here the threads split the work of the       */
+/* independent groups of a level, or of one large group's vectors, and     */
+/* every result is independent of the thread count:                        */
+/*   - element-wise loops write disjoint entries;                          */
+/*   - sums over more than RBLK values add fixed blocks of RBLK in order    */
+/*     and then the block sums in order (a single block: the plain         */
+/*     sequential sum);                                                     */
+/*   - recursive bisections run their two halves as tasks on disjoint      */
+/*     index ranges with disjoint scratch.                                  */
+/* ------------------------------------------------------------------------ */
+#define RBLK 65536
+#define TASK_MIN 32768
+
+int oracle_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+static int in_parallel(void) {
+#ifdef _OPENMP
+  return omp_in_parallel();
+#else
+  return 0;
+#endif
+}
+
+/* sum_{i<n} f(i) in fixed blocks of RBLK (see above) */
+#define BLOCKED_SUM(OUT, N, EXPR)                                               \
+  do {                                                                          \
+    ll n_ = (N), nb_ = (n_ + RBLK - 1) / RBLK;                                  \
+    if (nb_ <= 1) {                                                             \
+      double s_ = 0.0;                                                          \
+      for (ll i = 0; i < n_; i++) s_ += (EXPR);                                 \
+      OUT = s_;                                                                 \
+    } else {                                                                    \
+      double *pb_ = (double *)malloc((size_t)nb_ * sizeof(double));             \
+      _Pragma("omp parallel for schedule(static) if(!in_parallel())")           \
+      for (ll b_ = 0; b_ < nb_; b_++) {                                         \
+        ll e_ = (b_ + 1) * RBLK < n_ ? (b_ + 1) * RBLK : n_;                    \
+        double s_ = 0.0;                                                        \
+        for (ll i = b_ * RBLK; i < e_; i++) s_ += (EXPR);                       \
+        pb_[b_] = s_;                                                           \
+      }                                                                         \
+      double t_ = 0.0;                                                          \
+      for (ll b_ = 0; b_ < nb_; b_++) t_ += pb_[b_];                            \
+      free(pb_);                                                                \
+      OUT = t_;                                                                 \
+    }                                                                           \
+  } while (0)
 
 /* ------------------------------------------------------------------------ */
 /* Options: defaults src/parrsb.c:26-44, env overrides src/parrsb.c:48-77.   */
@@ -208,13 +269,18 @@ static int bbox_axis(const int *a, ll n, const double *cent, int ndim) {
 typedef struct {
   const double *cent; /* 3 per element */
   double *key;        /* scratch key per element */
-  int *tmp;
+  int *tmp;           /* scratch aligned with the order array a_base */
+  const int *a_base;
   int ndim;
 } geo_ctx;
 
+/* scratch for the index range starting at a: disjoint ranges get disjoint
+ * scratch, so the two halves of a bisection can run at the same time */
+#define TMP(g, a) ((g)->tmp + ((a) - (g)->a_base))
+
 static void sort_by_coord(int *a, ll n, geo_ctx *g, int axis) {
   for (ll i = 0; i < n; i++) g->key[a[i]] = g->cent[3 * (ll)a[i] + axis];
-  msort(a, g->tmp, n, g->key);
+  msort(a, TMP(g, a), n, g->key);
 }
 
 /* rcb_local (src/rcb.c:39-72): start/end are indices local to the rank. */
@@ -224,8 +290,10 @@ static void rcb_local(int *a, ll start, ll end, geo_ctx *g) {
   int axis = bbox_axis(a + start, size, g->cent, g->ndim);
   sort_by_coord(a + start, size, g, axis);
   ll mid = (start + end) / 2;
+#pragma omp task if(size >= TASK_MIN)
   rcb_local(a, start, mid, g);
   rcb_local(a, mid, end, g);
+#pragma omp taskwait
 }
 
 /* Recursive RCB over virtual ranks; leaves get rcb_local and their rank. */
@@ -242,8 +310,10 @@ static void rcb_rec(int *a, ll n, int p, int r0, geo_ctx *g, int *rank_of,
   sort_by_coord(a, n, g, axis);
   ll L = lower_count(n, p);
   int h = (p + 1) / 2;
+#pragma omp task if(n >= TASK_MIN)
   rcb_rec(a, L, h, r0, g, rank_of, do_local);
   rcb_rec(a + L, n - L, p - h, r0 + h, g, rank_of, do_local);
+#pragma omp taskwait
 }
 
 /* ------------------------------------------------------------------------ */
@@ -300,10 +370,12 @@ static void rib_local(int *a, ll start, ll end, geo_ctx *g) {
   ll size = end - start;
   if (size <= 1) return;
   rib_keys(a + start, size, g, 0);
-  msort(a + start, g->tmp, size, g->key);
+  msort(a + start, TMP(g, a + start), size, g->key);
   ll mid = (start + end) / 2;
+#pragma omp task if(size >= TASK_MIN)
   rib_local(a, start, mid, g);
   rib_local(a, mid, end, g);
+#pragma omp taskwait
 }
 
 static void rib_rec(int *a, ll n, int p, int r0, geo_ctx *g, int *rank_of,
@@ -316,11 +388,34 @@ static void rib_rec(int *a, ll n, int p, int r0, geo_ctx *g, int *rank_of,
     return;
   }
   rib_keys(a, n, g, 1);
-  msort(a, g->tmp, n, g->key);
+  msort(a, TMP(g, a), n, g->key);
   ll L = lower_count(n, p);
   int h = (p + 1) / 2;
+#pragma omp task if(n >= TASK_MIN)
   rib_rec(a, L, h, r0, g, rank_of, do_local);
   rib_rec(a + L, n - L, p - h, r0 + h, g, rank_of, do_local);
+#pragma omp taskwait
+}
+
+/* Run a recursive bisection on the calling thread's team: inside a parallel
+ * region the tasks join it; outside, a region is opened for them. */
+static void rcb_run(int *a, ll n, int p, int r0, geo_ctx *g, int *rank_of, int do_local) {
+  if (in_parallel()) {
+    rcb_rec(a, n, p, r0, g, rank_of, do_local);
+    return;
+  }
+#pragma omp parallel
+#pragma omp single
+  rcb_rec(a, n, p, r0, g, rank_of, do_local);
+}
+static void rib_run(int *a, ll n, int p, int r0, geo_ctx *g, int *rank_of, int do_local) {
+  if (in_parallel()) {
+    rib_rec(a, n, p, r0, g, rank_of, do_local);
+    return;
+  }
+#pragma omp parallel
+#pragma omp single
+  rib_rec(a, n, p, r0, g, rank_of, do_local);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -352,18 +447,91 @@ static void csr_free(csr_t *m) {
   m->rowptr = NULL, m->col = NULL, m->w = NULL;
 }
 
+/* Stable LSD radix sort of slots by vertex id (16-bit digits; a digit that
+ * is the same for every slot is skipped).  Equals qsort by (vid, slot) when
+ * the input is in slot order. */
+static void radix_slots(slot_t *s, ll n) {
+  if (n < 2) return;
+  slot_t *t = (slot_t *)malloc((size_t)n * sizeof(slot_t));
+  ll *cnt = (ll *)malloc((size_t)65536 * sizeof(ll));
+  slot_t *src = s, *dst = t;
+  for (int shift = 0; shift < 64; shift += 16) {
+    memset(cnt, 0, (size_t)65536 * sizeof(ll));
+    for (ll i = 0; i < n; i++)
+      cnt[(((unsigned long long)src[i].vid ^ 0x8000000000000000ull) >> shift) & 0xFFFF]++;
+    int trivial = 0;
+    for (int d = 0; d < 65536; d++)
+      if (cnt[d] == n) trivial = 1;
+    if (trivial) continue;
+    ll acc = 0;
+    for (int d = 0; d < 65536; d++) {
+      ll c = cnt[d];
+      cnt[d] = acc;
+      acc += c;
+    }
+    for (ll i = 0; i < n; i++) {
+      unsigned d = (unsigned)((((unsigned long long)src[i].vid ^ 0x8000000000000000ull) >> shift) &
+                              0xFFFF);
+      dst[cnt[d]++] = src[i];
+    }
+    slot_t *x = src;
+    src = dst, dst = x;
+  }
+  if (src != s) memcpy(s, src, (size_t)n * sizeof(slot_t));
+  free(t), free(cnt);
+}
+
 /* Graph of the elements elems[0..n) (local index = position); vertex ids
- * of element e are vtx[e*nv .. e*nv+nv). */
+ * of element e are vtx[e*nv .. e*nv+nv).  Row a lists every b != a sharing
+ * a vertex with a, columns ascending, weight = number of (slot of a, slot
+ * of b) pairs with equal ids.  Rows are independent: counted, then filled,
+ * in parallel. */
+static ll graph_row(ll a, int nv, const slot_t *s, const ll *gs, const ll *ge, const ll *inv,
+                    int **bufp, ll *bcapp, int *col, int *w) {
+  ll nb = 0;
+  int *buf = *bufp;
+  for (int k = 0; k < nv; k++) {
+    ll pos = inv[a * nv + k];
+    ll len = ge[pos] - gs[pos];
+    if (nb + len > *bcapp) {
+      *bcapp = 2 * (nb + len) + 64;
+      buf = (int *)realloc(buf, (size_t)*bcapp * sizeof(int));
+      *bufp = buf;
+    }
+    for (ll q = gs[pos]; q < ge[pos]; q++) {
+      int b = s[q].slot / nv;
+      if (b != a) buf[nb++] = b;
+    }
+  }
+  /* insertion sort, then run-length = weight */
+  for (ll i = 1; i < nb; i++) {
+    int v = buf[i];
+    ll j = i - 1;
+    while (j >= 0 && buf[j] > v) buf[j + 1] = buf[j], j--;
+    buf[j + 1] = v;
+  }
+  ll nnz = 0;
+  for (ll i = 0; i < nb;) {
+    ll j = i + 1;
+    while (j < nb && buf[j] == buf[i]) j++;
+    if (col) col[nnz] = buf[i], w[nnz] = (int)(j - i);
+    nnz++;
+    i = j;
+  }
+  return nnz;
+}
+
 static void build_graph(csr_t *m, const int *elems, ll n, const long long *vtx,
                         int nv) {
   ll ns = n * nv;
   slot_t *s = (slot_t *)malloc((size_t)(ns > 0 ? ns : 1) * sizeof(slot_t));
+#pragma omp parallel for schedule(static) if(!in_parallel() && n >= TASK_MIN)
   for (ll i = 0; i < n; i++)
     for (int k = 0; k < nv; k++) {
       s[i * nv + k].vid = vtx[(ll)elems[i] * nv + k];
       s[i * nv + k].slot = (int)(i * nv + k);
     }
-  qsort(s, (size_t)ns, sizeof(slot_t), cmp_slot);
+  radix_slots(s, ns);
   ll *gs = (ll *)malloc((size_t)(ns > 0 ? ns : 1) * sizeof(ll));
   ll *ge = (ll *)malloc((size_t)(ns > 0 ? ns : 1) * sizeof(ll));
   ll *inv = (ll *)malloc((size_t)(ns > 0 ? ns : 1) * sizeof(ll));
@@ -375,51 +543,35 @@ static void build_graph(csr_t *m, const int *elems, ll n, const long long *vtx,
   }
   m->n = n;
   m->rowptr = (ll *)malloc((size_t)(n + 1) * sizeof(ll));
-  ll cap = 32 * n + 16, nnz = 0;
-  m->col = (int *)malloc((size_t)cap * sizeof(int));
-  m->w = (int *)malloc((size_t)cap * sizeof(int));
-  int *buf = NULL;
-  ll bcap = 0;
   m->rowptr[0] = 0;
-  for (ll a = 0; a < n; a++) {
-    ll nb = 0;
-    for (int k = 0; k < nv; k++) {
-      ll pos = inv[a * nv + k];
-      ll len = ge[pos] - gs[pos];
-      if (nb + len > bcap) {
-        bcap = 2 * (nb + len) + 64;
-        buf = (int *)realloc(buf, (size_t)bcap * sizeof(int));
-      }
-      for (ll q = gs[pos]; q < ge[pos]; q++) {
-        int b = s[q].slot / nv;
-        if (b != a) buf[nb++] = b;
-      }
-    }
-    /* insertion sort, then run-length = weight */
-    for (ll i = 1; i < nb; i++) {
-      int v = buf[i];
-      ll j = i - 1;
-      while (j >= 0 && buf[j] > v) buf[j + 1] = buf[j], j--;
-      buf[j + 1] = v;
-    }
-    for (ll i = 0; i < nb;) {
-      ll j = i + 1;
-      while (j < nb && buf[j] == buf[i]) j++;
-      if (nnz >= cap) {
-        cap *= 2;
-        m->col = (int *)realloc(m->col, (size_t)cap * sizeof(int));
-        m->w = (int *)realloc(m->w, (size_t)cap * sizeof(int));
-      }
-      m->col[nnz] = buf[i], m->w[nnz] = (int)(j - i), nnz++;
-      i = j;
-    }
-    m->rowptr[a + 1] = nnz;
+#pragma omp parallel if(!in_parallel() && n >= TASK_MIN)
+  {
+    int *buf = NULL;
+    ll bcap = 0;
+#pragma omp for schedule(static)
+    for (ll a = 0; a < n; a++)
+      m->rowptr[a + 1] = graph_row(a, nv, s, gs, ge, inv, &buf, &bcap, NULL, NULL);
+    free(buf);
   }
-  free(buf), free(s), free(gs), free(ge), free(inv);
+  for (ll a = 0; a < n; a++) m->rowptr[a + 1] += m->rowptr[a];
+  ll nnz = m->rowptr[n];
+  m->col = (int *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int));
+  m->w = (int *)malloc((size_t)(nnz > 0 ? nnz : 1) * sizeof(int));
+#pragma omp parallel if(!in_parallel() && n >= TASK_MIN)
+  {
+    int *buf = NULL;
+    ll bcap = 0;
+#pragma omp for schedule(static)
+    for (ll a = 0; a < n; a++)
+      graph_row(a, nv, s, gs, ge, inv, &buf, &bcap, m->col + m->rowptr[a], m->w + m->rowptr[a]);
+    free(buf);
+  }
+  free(s), free(gs), free(ge), free(inv);
 }
 
 /* y = L x in the difference form y_a = sum_b w_ab (x_a - x_b). */
 static void lap_apply(double *y, const double *x, const csr_t *m) {
+#pragma omp parallel for schedule(static) if(!in_parallel() && m->n >= TASK_MIN)
   for (ll a = 0; a < m->n; a++) {
     double acc = 0.0;
     for (ll q = m->rowptr[a]; q < m->rowptr[a + 1]; q++)
@@ -463,15 +615,18 @@ long long oracle_dual_graph(long long *rowptr, int *col, int *w, long long cap,
 /* lanczos_aux :434-511, lanczos :513-561, fiedler :563-621.                 */
 /* ------------------------------------------------------------------------ */
 static double dot(const double *y, const double *x, ll n) {
-  double r = 0.0;
-  for (ll i = 0; i < n; i++) r += x[i] * y[i];
+  double r;
+  BLOCKED_SUM(r, n, x[i] * y[i]);
   return r;
 }
 
+#define PAR_FOR _Pragma("omp parallel for schedule(static) if(!in_parallel() && n >= TASK_MIN)")
+
 static void ortho(double *q, ll n) {
-  double sum = 0.0;
-  for (ll i = 0; i < n; i++) sum += q[i];
+  double sum;
+  BLOCKED_SUM(sum, n, q[i]);
   sum /= (double)n;
+  PAR_FOR
   for (ll i = 0; i < n; i++) q[i] -= sum;
 }
 
@@ -566,26 +721,31 @@ static int lanczos_aux(double *diag, double *upper, double *rr, ll n,
                        const csr_t *L) {
   double *r = (double *)calloc((size_t)(3 * n), sizeof(double));
   double *p = r + n, *w = p + n;
+  PAR_FOR
   for (ll i = 0; i < n; i++) r[i] = f[i];
   ortho(r, n);
   double rtz1 = 1, pap = 0, alpha, beta, rtz2, pap_old;
   double rtr = dot(r, r, n);
   double rnorm = sqrt(rtr), rtol = rnorm * tol;
   double rni = 1.0 / rnorm;
+  PAR_FOR
   for (ll i = 0; i < n; i++) rr[i] = r[i] * rni;
   int iter;
   for (iter = 0; iter < niter; iter++) {
     rtz2 = rtz1, rtz1 = rtr;
     beta = rtz1 / rtz2;
     if (iter == 0) beta = 0.0;
+    PAR_FOR
     for (ll i = 0; i < n; i++) p[i] = beta * p[i] + r[i];
     ortho(p, n);
     lap_apply(w, p, L);
     pap_old = pap, pap = dot(w, p, n);
     alpha = rtz1 / pap;
+    PAR_FOR
     for (ll i = 0; i < n; i++) r[i] = r[i] - alpha * w[i];
     rtr = dot(r, r, n);
     rnorm = sqrt(rtr), rni = 1.0 / rnorm;
+    PAR_FOR
     for (ll i = 0; i < n; i++) rr[(iter + 1) * n + i] = r[i] * rni;
     if (iter == 0) {
       diag[iter] = pap / rtz1;
@@ -619,12 +779,14 @@ static int lanczos(double *fiedler, ll n, double *initv, const csr_t *L,
     int eValMinI = 0;
     for (int i = 1; i < iter; i++)
       if (fabs(eValues[i]) < eValMin) eValMin = fabs(eValues[i]), eValMinI = i;
+    PAR_FOR
     for (ll i = 0; i < n; i++) {
       fiedler[i] = 0.0;
       for (int j = 0; j < iter; j++)
         fiedler[i] += rr[(ll)j * n + i] * eVectors[eValMinI * iter + j];
     }
     ortho(fiedler, n);
+    PAR_FOR
     for (ll i = 0; i < n; i++) initv[i] = fiedler[i];
   }
   free(alpha), free(rr), free(eVectors), free(eValues);
@@ -637,6 +799,7 @@ static int fiedler_group(double *f, const csr_t *L, int miter, int mpass,
                          double tol, int *passes_out) {
   ll n = L->n;
   double *initv = (double *)calloc((size_t)n, sizeof(double));
+  PAR_FOR
   for (ll i = 0; i < n; i++) {
     initv[i] = i + 1.0;
     if (i < n / 2) initv[i] += 1000 * n;
@@ -644,20 +807,24 @@ static int fiedler_group(double *f, const csr_t *L, int miter, int mpass,
   ortho(initv, n);
   double rtr = dot(initv, initv, n);
   double rni = 1.0 / sqrt(rtr);
+  PAR_FOR
   for (ll i = 0; i < n; i++) initv[i] *= rni;
   int iter = lanczos(f, n, initv, L, miter, mpass, tol, passes_out);
-  double norm = 0;
-  for (ll i = 0; i < n; i++) norm += f[i] * f[i];
+  double norm;
+  BLOCKED_SUM(norm, n, f[i] * f[i]);
   double normi = 1.0 / sqrt(norm);
+  PAR_FOR
   for (ll i = 0; i < n; i++) f[i] *= normi;
   /* Canonical orientation (shared with the GPU): the reference's sign comes
    * from tqli's accumulated rotations; here f is oriented like the step of
    * the start vector, sum_i f_i s_i >= 0 with s_i = +1 for i < n/2 and -1
    * otherwise.  A flip swaps the two halves of the bisection. */
-  double orient = 0.0;
-  for (ll i = 0; i < n; i++) orient += (i < n / 2) ? f[i] : -f[i];
-  if (orient < 0.0)
+  double orient;
+  BLOCKED_SUM(orient, n, (i < n / 2) ? f[i] : -f[i]);
+  if (orient < 0.0) {
+    PAR_FOR
     for (ll i = 0; i < n; i++) f[i] = -f[i];
+  }
   free(initv);
   return iter;
 }
@@ -668,11 +835,8 @@ static double fiedler_resid(const double *f, const csr_t *L) {
   double *y = (double *)malloc((size_t)(n > 0 ? n : 1) * sizeof(double));
   lap_apply(y, f, L);
   double ff = dot(f, f, n), fLf = dot(f, y, n);
-  double rho = fLf / ff, s = 0.0;
-  for (ll i = 0; i < n; i++) {
-    double t = y[i] - rho * f[i];
-    s += t * t;
-  }
+  double rho = fLf / ff, s;
+  BLOCKED_SUM(s, n, (y[i] - rho * f[i]) * (y[i] - rho * f[i]));
   free(y);
   return sqrt(s) / sqrt(ff);
 }
@@ -708,7 +872,7 @@ static int count_components(const int *elems, ll n, const long long *vtx,
       s[i * nv + k].vid = vtx[(ll)elems[i] * nv + k];
       s[i * nv + k].slot = (int)(i * nv + k);
     }
-  qsort(s, (size_t)ns, sizeof(slot_t), cmp_slot);
+  radix_slots(s, ns);
   int *par = (int *)malloc((size_t)n * sizeof(int));
   for (ll i = 0; i < n; i++) par[i] = (int)i;
   for (ll i = 0; i < ns;) {
@@ -842,6 +1006,127 @@ typedef struct {
   int p, r0;
 } seg_t;
 
+/* Result of one group's bisection (merged into the info in group order). */
+typedef struct {
+  ll iters, L;
+  int unconverged, comps;
+  double resid;
+} bis_t;
+
+/* One group's cut (the body of rsb's loop, src/rsb.c:276-343): pre-partition,
+ * Fiedler vector, sort, component count, balance.  a: the group's order,
+ * tmp: scratch aligned with a; key / fied / moved are indexed by element
+ * id (disjoint between groups). */
+static void rsb_group(int *a, int *tmp, ll n, int p, const long long *vtx, int nv,
+                      const double *cent, int ndim, const parrsb_options *o, double *key,
+                      double *fied, char *moved, int want_info, bis_t *out) {
+  geo_ctx g = {cent, key, tmp, a, ndim};
+  /* pre-partition (src/rsb.c:282-292) */
+  if (o->rsb_pre == 0)
+    msort_int(a, tmp, n);
+  else if (o->rsb_pre == 1)
+    rcb_run(a, n, p, 0, &g, NULL, 1);
+  else if (o->rsb_pre == 2)
+    rib_run(a, n, p, 0, &g, NULL, 1);
+  /* Fiedler vector (src/rsb.c:300-302) */
+  csr_t Lg;
+  build_graph(&Lg, a, n, vtx, nv);
+  double *f = (double *)calloc((size_t)n, sizeof(double));
+  int passes = 0;
+  int miter = o->rsb_max_iter, mpass = o->rsb_max_passes;
+  int it = fiedler_group(f, &Lg, miter, mpass, o->rsb_tol, &passes);
+  memset(out, 0, sizeof(*out));
+  out->iters = it;
+  if (want_info) {
+    int mi = (int)(n < miter ? n : miter);
+    out->unconverged = (it == mi * mpass);
+    out->resid = fiedler_resid(f, &Lg);
+  }
+  csr_free(&Lg);
+  for (ll i = 0; i < n; i++) fied[a[i]] = f[i];
+  free(f);
+  /* sort by Fiedler value (src/rsb.c:307-309) */
+  msort(a, tmp, n, fied);
+  ll L = lower_count(n, p);
+  /* components of each half (src/rsb.c:319-327), count only */
+  if (o->find_disconnected_comps && want_info) {
+    int c0 = count_components(a, L, vtx, nv);
+    int c1 = count_components(a + L, n - L, vtx, nv);
+    out->comps = c0 > c1 ? c0 : c1;
+  }
+  /* balance (src/rsb.c:333-335) */
+  balance(a, n, p, &L, fied, vtx, nv, tmp, key, moved);
+  out->L = L;
+}
+
+/* One level of RSB over all its segments.  seg_in[k] = (start, n, p, r0) of
+ * segment k in the order a; seg_out receives the next level's segments (two
+ * per segment with p > 1 and n > 0, the segment itself otherwise); returns
+ * their number.  Groups run in parallel when there are at least as many as
+ * threads, otherwise one after the other with their vectors split among the
+ * threads; the result is the same either way. */
+int oracle_rsb_level(int *a, const long long *seg_in, int nseg, long long *seg_out,
+                     const long long *vtx, const double *cent, int nel, int nv,
+                     const parrsb_options *o, oracle_rsb_info *info) {
+  int ndim = (nv == 8) ? 3 : 2;
+  int *tmp = (int *)malloc((size_t)(nel > 0 ? nel : 1) * sizeof(int));
+  double *key = (double *)malloc((size_t)(nel > 0 ? nel : 1) * sizeof(double));
+  double *fied = (double *)calloc((size_t)(nel > 0 ? nel : 1), sizeof(double));
+  char *moved = (char *)calloc((size_t)(nel > 0 ? nel : 1), 1);
+  int *act = (int *)malloc((size_t)(nseg > 0 ? nseg : 1) * sizeof(int));
+  bis_t *res = (bis_t *)calloc((size_t)(nseg > 0 ? nseg : 1), sizeof(bis_t));
+  int na = 0;
+  for (int k = 0; k < nseg; k++)
+    if (seg_in[4 * k + 2] > 1 && seg_in[4 * k + 1] > 0) act[na++] = k;
+  int nthr = oracle_threads(0);
+  int want = info != NULL;
+  if (na >= nthr) {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int q = 0; q < na; q++) {
+      const long long *sg = seg_in + 4 * act[q];
+      rsb_group(a + sg[0], tmp + sg[0], sg[1], (int)sg[2], vtx, nv, cent, ndim, o, key, fied,
+                moved, want, &res[act[q]]);
+    }
+  } else {
+    for (int q = 0; q < na; q++) {
+      const long long *sg = seg_in + 4 * act[q];
+      rsb_group(a + sg[0], tmp + sg[0], sg[1], (int)sg[2], vtx, nv, cent, ndim, o, key, fied,
+                moved, want, &res[act[q]]);
+    }
+  }
+  int nn = 0;
+  for (int k = 0; k < nseg; k++) {
+    const long long *sg = seg_in + 4 * k;
+    long long *d = seg_out + 4 * nn;
+    if (!(sg[2] > 1 && sg[1] > 0)) {
+      d[0] = sg[0], d[1] = sg[1], d[2] = sg[2], d[3] = sg[3];
+      nn++;
+      continue;
+    }
+    const bis_t *r = &res[k];
+    if (info) {
+      info->total_iters += r->iters;
+      info->row_iters += r->iters * sg[1];
+      info->nbisect++;
+      info->unconverged += r->unconverged;
+      if (r->resid > info->max_resid) info->max_resid = r->resid;
+      if (r->comps > info->max_components) info->max_components = r->comps;
+    }
+    int h = (int)((sg[2] + 1) / 2);
+    d[0] = sg[0], d[1] = r->L, d[2] = h, d[3] = sg[3];
+    d[4] = sg[0] + r->L, d[5] = sg[1] - r->L, d[6] = sg[2] - h, d[7] = sg[3] + h;
+    nn += 2;
+  }
+  if (info && na > 0) info->levels++;
+  free(tmp), free(key), free(fied), free(moved), free(act), free(res);
+  return nn;
+}
+
+/* ------------------------------------------------------------------------ */
+/* parrsb_part_mesh: src/parrsb.c:853-906 -> parrsb_part_mesh_v0 :236-290,  */
+/* rsb src/rsb.c:262-350 (one node: level 0 has no cuts, the last level     */
+/* makes ceil(log2 P) cuts, get_level_cuts :244-260, get_bin :231-242).     */
+/* ------------------------------------------------------------------------ */
 int oracle_part_mesh(int *part, int *order, const long long *vtx,
                      const double *xyz, int nel, int nv,
                      parrsb_options *options, int nparts,
@@ -865,82 +1150,29 @@ int oracle_part_mesh(int *part, int *order, const long long *vtx,
   int *a = (int *)malloc((size_t)nel * sizeof(int));
   int *tmp = (int *)malloc((size_t)nel * sizeof(int));
   double *key = (double *)malloc((size_t)nel * sizeof(double));
-  double *fied = (double *)calloc((size_t)nel, sizeof(double));
-  char *moved = (char *)calloc((size_t)nel, 1);
   for (int i = 0; i < nel; i++) a[i] = i;
-  geo_ctx g = {cent, key, tmp, ndim};
+  geo_ctx g = {cent, key, tmp, a, ndim};
 
   int rc = PARRSB_OK;
   if (options->partitioner == 1) {
-    rcb_rec(a, nel, P, 0, &g, part, 1);
+    rcb_run(a, nel, P, 0, &g, part, 1);
   } else if (options->partitioner == 2) {
-    rib_rec(a, nel, P, 0, &g, part, 1);
+    rib_run(a, nel, P, 0, &g, part, 1);
   } else if (options->partitioner == 0) {
     int ncuts = 0;
     for (int pw = 1; pw < P; pw <<= 1) ncuts++;
-    seg_t *segs = (seg_t *)malloc((size_t)2 * P * sizeof(seg_t));
-    seg_t *nsegs = (seg_t *)malloc((size_t)2 * P * sizeof(seg_t));
+    long long *segs = (long long *)malloc((size_t)8 * P * sizeof(long long));
+    long long *nsegs = (long long *)malloc((size_t)8 * P * sizeof(long long));
     int nseg = 1;
-    segs[0].s = 0, segs[0].n = nel, segs[0].p = P, segs[0].r0 = 0;
-    int miter = options->rsb_max_iter, mpass = options->rsb_max_passes;
+    segs[0] = 0, segs[1] = nel, segs[2] = P, segs[3] = 0;
     for (int cut = 0; cut < ncuts; cut++) {
-      int nn = 0;
-      for (int si = 0; si < nseg; si++) {
-        seg_t sg = segs[si];
-        if (sg.p <= 1 || sg.n == 0) {
-          nsegs[nn++] = sg;
-          continue;
-        }
-        int *sa = a + sg.s;
-        /* pre-partition (src/rsb.c:282-292) */
-        if (options->rsb_pre == 0)
-          msort_int(sa, tmp, sg.n);
-        else if (options->rsb_pre == 1)
-          rcb_rec(sa, sg.n, sg.p, 0, &g, NULL, 1);
-        else if (options->rsb_pre == 2)
-          rib_rec(sa, sg.n, sg.p, 0, &g, NULL, 1);
-        /* Fiedler vector (src/rsb.c:300-302) */
-        csr_t Lg;
-        build_graph(&Lg, sa, sg.n, vtx, nv);
-        double *f = (double *)calloc((size_t)sg.n, sizeof(double));
-        int passes = 0;
-        int it = fiedler_group(f, &Lg, miter, mpass, options->rsb_tol, &passes);
-        if (info) {
-          info->total_iters += it;
-          info->nbisect++;
-          int mi = (int)(sg.n < miter ? sg.n : miter);
-          if (it == mi * mpass) info->unconverged++;
-          double rsd = fiedler_resid(f, &Lg);
-          if (rsd > info->max_resid) info->max_resid = rsd;
-        }
-        csr_free(&Lg);
-        for (ll i = 0; i < sg.n; i++) fied[sa[i]] = f[i];
-        free(f);
-        /* sort by Fiedler value (src/rsb.c:307-309) */
-        msort(sa, tmp, sg.n, fied);
-        ll L = lower_count(sg.n, sg.p);
-        int h = (sg.p + 1) / 2;
-        /* components of each half (src/rsb.c:319-327), count only */
-        if (options->find_disconnected_comps && info) {
-          int c0 = count_components(sa, L, vtx, nv);
-          int c1 = count_components(sa + L, sg.n - L, vtx, nv);
-          if (c0 > info->max_components) info->max_components = c0;
-          if (c1 > info->max_components) info->max_components = c1;
-        }
-        /* balance (src/rsb.c:333-335) */
-        balance(sa, sg.n, sg.p, &L, fied, vtx, nv, tmp, key, moved);
-        nsegs[nn].s = sg.s, nsegs[nn].n = L, nsegs[nn].p = h, nsegs[nn].r0 = sg.r0;
-        nn++;
-        nsegs[nn].s = sg.s + L, nsegs[nn].n = sg.n - L, nsegs[nn].p = sg.p - h;
-        nsegs[nn].r0 = sg.r0 + h;
-        nn++;
-      }
-      seg_t *t = segs;
-      segs = nsegs, nsegs = t, nseg = nn;
-      if (info) info->levels++;
+      nseg = oracle_rsb_level(a, segs, nseg, nsegs, vtx, cent, nel, nv, options, info);
+      long long *t = segs;
+      segs = nsegs, nsegs = t;
     }
     for (int si = 0; si < nseg; si++)
-      for (ll i = 0; i < segs[si].n; i++) part[a[segs[si].s + i]] = segs[si].r0;
+      for (ll i = 0; i < segs[4 * si + 1]; i++)
+        part[a[segs[4 * si] + i]] = (int)segs[4 * si + 3];
     free(segs), free(nsegs);
   } else {
     /* unknown partitioner: elements stay on their load_balance rank
@@ -958,7 +1190,7 @@ int oracle_part_mesh(int *part, int *order, const long long *vtx,
     }
   }
   if (order) memcpy(order, a, (size_t)nel * sizeof(int));
-  free(cent), free(a), free(tmp), free(key), free(fied), free(moved);
+  free(cent), free(a), free(tmp), free(key);
   return rc;
 }
 

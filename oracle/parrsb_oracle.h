@@ -35,6 +35,7 @@ typedef struct {
   int max_components;      /* max component count over halves */
   double max_resid;        /* max FP64 ||Lf - rho f||/||f|| over bisections */
   int levels;              /* cuts performed */
+  long long row_iters;     /* Lanczos steps x group rows, summed */
 } oracle_rsb_info;
 
 /* parrsb_part_mesh with nparts virtual ranks.  order (optional, nel) gets
@@ -43,6 +44,19 @@ int oracle_part_mesh(int *part, int *order, const long long *vtx,
                      const double *xyz, int nel, int nv,
                      parrsb_options *options, int nparts,
                      oracle_rsb_info *info);
+
+/* One RSB level (one cut of every segment; the loop body of rsb,
+ * src/rsb.c:276-343) on the element order a[nel].  seg_in: nseg records
+ * (start, n, p, r0) as long long; seg_out (room for 2 * nseg records)
+ * receives the next level's segments; returns their number.  cent: 3 per
+ * element (oracle_centroids).  info (optional) accumulates. */
+int oracle_rsb_level(int *a, const long long *seg_in, int nseg, long long *seg_out,
+                     const long long *vtx, const double *cent, int nel, int nv,
+                     const parrsb_options *o, oracle_rsb_info *info);
+
+/* Host threads used by the oracle (OpenMP builds; 1 otherwise).  n > 0 sets
+ * the count; returns the count in effect.  Results do not depend on it. */
+int oracle_threads(int n);
 
 /* parrsb_conn_mesh on one rank.  heapsort_mode = 1 restates the reference's
  * per-segment heapsort (src/con-unique-vertices.c:6-58); 0 uses stable sorts

@@ -30,7 +30,9 @@ EXPORTS = ["parrsb_default_options", "parrsb_part_mesh", "parrsb_conn_mesh",
            "parrsb_conn_mesh_device", "parrsb_get_stats", "parrsb_part_quality",
            "parrsb_gpu_finalize", "parrsb_fiedler_groups", "parrsb_part_mesh_seq",
            "parrsb_read_mesh", "parrsb_dump_con", "parrsb_dump_map",
-           "parrsb_part_mesh_rcb_noalloc", "parrsb_dual_graph", "parrsb_components"]
+           "parrsb_part_mesh_rcb_noalloc", "parrsb_dual_graph", "parrsb_components",
+           "parrsb_warm_install", "parrsb_warm_batch_create", "parrsb_warm_batch_destroy",
+           "parrsb_warm_batch_features", "parrsb_warm_batch_step", "parrsb_warm_adam"]
 
 
 class ParrsbError(RuntimeError):
@@ -55,7 +57,12 @@ class Stats(ctypes.Structure):
                 ("nnz", ctypes.c_longlong),
                 ("gencon_segments", ctypes.c_longlong),
                 ("lanczos_ms", ctypes.c_double * 6),
-                ("lanczos_passes", ctypes.c_longlong)]
+                ("lanczos_passes", ctypes.c_longlong),
+                ("warm_tried", ctypes.c_longlong),
+                ("warm_used", ctypes.c_longlong),
+                ("warm_ms", ctypes.c_double),
+                ("start_resid_fallback", ctypes.c_double),
+                ("start_resid_warm", ctypes.c_double)]
 
     def as_dict(self):
         d = {}
@@ -118,6 +125,13 @@ def library(build_if_missing=False):
     L.parrsb_dual_graph.restype = ctypes.c_int
     L.parrsb_components.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.parrsb_components.restype = ctypes.c_int
+    L.parrsb_warm_install.argtypes = [P]
+    L.parrsb_warm_batch_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), P, P, P,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.parrsb_warm_batch_destroy.argtypes = [P]
+    L.parrsb_warm_batch_features.argtypes = [P, P]
+    L.parrsb_warm_batch_step.argtypes = [P, P, P, P, P, ctypes.POINTER(ctypes.c_double)]
+    L.parrsb_warm_adam.argtypes = [P, P, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_float]
     _lib = L
     return L
 

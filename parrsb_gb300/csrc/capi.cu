@@ -18,6 +18,7 @@
 #include "gencon.cuh"
 #include "periodic.cuh"
 #include "rsb.cuh"
+#include "warm.cuh"
 
 extern "C" {
 parrsb_options parrsb_default_options = {
@@ -174,6 +175,23 @@ int prepare_options(const long long *vtx, const double *xyz, int nel, int nv,
   return PARRSB_OK;
 }
 
+// PARRSB_GPU_WARM_WEIGHTS=<file>: the warm-start network's parameters as
+// raw little-endian FP32 (MP_NPARAM values), installed on the current device
+// the first time a call asks for the warm start there.
+void load_warm_weights_from_env() {
+  if (warm_net_ready()) return;
+  const char *path = getenv("PARRSB_GPU_WARM_WEIGHTS");
+  if (!path) throw ArgError{PARRSB_ERR_ARGS, "PARRSB_GPU_WARM=1 without an installed network "
+                                             "(parrsb_warm_install or PARRSB_GPU_WARM_WEIGHTS)"};
+  FILE *fp = fopen(path, "rb");
+  if (!fp) throw ArgError{PARRSB_ERR_ARGS, "cannot open PARRSB_GPU_WARM_WEIGHTS"};
+  std::vector<float> w(MP_NPARAM);
+  const size_t got = fread(w.data(), sizeof(float), MP_NPARAM, fp);
+  fclose(fp);
+  if (got != (size_t)MP_NPARAM) throw ArgError{PARRSB_ERR_ARGS, "PARRSB_GPU_WARM_WEIGHTS too short"};
+  warm_net_install(w.data());
+}
+
 __global__ void k_block_part(int *part, ll nel, int nparts) {
   ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= nel) return;
@@ -269,6 +287,11 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.check_resid = env_int("PARRSB_GPU_CHECK_RESID", 1);
     ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
     ro.batched = env_int("PARRSB_GPU_BATCHED", 1);
+    ro.start = env_int("PARRSB_GPU_START", 0);
+    ro.warm = env_int("PARRSB_GPU_WARM", 0);
+    ro.warm_min = env_int("PARRSB_GPU_WARM_MIN", 0);
+    ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
+    if (ro.warm) load_warm_weights_from_env();
     rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq, sg);
     sync();
   } else {

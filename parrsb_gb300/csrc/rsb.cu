@@ -26,6 +26,7 @@
 #include <array>
 
 #include "rsb.cuh"
+#include "warm.cuh"
 
 namespace prsb {
 
@@ -259,6 +260,7 @@ struct GState {
   ll start, n;
   ll total_iters;
   int tile0, ntiles, miter, run, iters, done, active, npass;
+  int warm;  // start from the learned prediction (else the fallback start)
 };
 
 __device__ __forceinline__ double block_sum(double v, double *sh) {
@@ -303,7 +305,9 @@ enum FinOp {
   FIN_NORM,
   FIN_RESID1,
   FIN_RESID2,
-  FIN_ORIENT
+  FIN_ORIENT,
+  FIN_PASS_END_R,  // pass end when the eigen-residual decides the restarts
+  FIN_RESID_GATE   // residual of the Ritz vector; restart while above tol
 };
 
 // One block per group: reduce the group's tile partials in a fixed order and
@@ -388,6 +392,14 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     s.active = (s.iters == s.miter && s.npass < mpass) ? 1 : 0;
     if (s.active) atomicOr(any_active, 1);
     atomicMax(any_active + 1, s.iters);
+  } else if (OP == FIN_PASS_END_R) {
+    s.total_iters += s.iters;
+    s.npass += 1;
+    atomicMax(any_active + 1, s.iters);  // active stays set until FIN_RESID_GATE
+  } else if (OP == FIN_RESID_GATE) {
+    s.resid = __ddiv_rn(__dsqrt_rn(tot[0]), __dsqrt_rn(s.ff));
+    s.active = (!(s.resid <= tol) && s.npass < mpass) ? 1 : 0;
+    if (s.active) atomicOr(any_active, 1);
   } else if (OP == FIN_NORM) {
     s.c = __ddiv_rn(1.0, __dsqrt_rn(tot[0]));
   } else if (OP == FIN_RESID1) {
@@ -463,8 +475,21 @@ enum TileMode {
   TM_RESID1 = 10,    // y = L f in FP64 -> y64; sums f.y, f.f
   TM_RESID2 = 11,    // sum (y - rho f)^2
   TM_SUM_F_WARM = 12, // same as TM_SUM_F but for a warm start vector
-  TM_ORIENT = 13      // sum s_i f_i, s = +1 on the first half of the group, -1 after
+  TM_ORIENT = 13,     // sum s_i f_i, s = +1 on the first half of the group, -1 after
+  TM_LOAD_Y = 14,     // f = y (FP64 per position, passed as y64)
+  TM_RANDOM = 15,     // f = seeded uniform values in [-1, 1)
+  TM_SELECT = 16      // groups without the warm flag: f = V (the saved fallback)
 };
+
+// SplitMix64 (Steele, Lea and Flood, 2014): the seeded random start vector
+// of position li of a group, uniform in [-1, 1).
+__device__ __forceinline__ double random_start(ll li) {
+  unsigned long long z = (unsigned long long)li * 0x9E3779B97F4A7C15ull + 0x2545F4914F6CDD1Dull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
 
 // Canonical per-tile reductions.  A tile's rows are cut into 32-row chunks
 // aligned to the ELL slices; a warp owns whole chunks (lane = row % 32), a
@@ -556,7 +581,8 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   const ll b = tbeg[t], e = tend[t];
   const ll c0 = b >> 5;
   const int nc = (int)(((e - 1) >> 5) - c0 + 1);
-  constexpr bool has_sum = !(MODE == TM_IV_WRITE || MODE == TM_SUB_C || MODE == TM_SCALE_F);
+  constexpr bool has_sum = !(MODE == TM_IV_WRITE || MODE == TM_SUB_C || MODE == TM_SCALE_F ||
+                             MODE == TM_LOAD_Y || MODE == TM_RANDOM || MODE == TM_SELECT);
   constexpr bool fp64_term = (MODE == TM_IV_SUM || MODE == TM_IV_SQ || MODE == TM_RESID1 ||
                               MODE == TM_RESID2);
   for (int q = warp; q < nc; q += nw) {
@@ -587,6 +613,12 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
         tv.set((i - s.start) < s.n / 2 ? f[i] : -f[i]);
       } else if (MODE == TM_SCALE_F) {
         f[i] = (VT)((double)f[i] * s.c);
+      } else if (MODE == TM_LOAD_Y) {
+        f[i] = (VT)y64[i];
+      } else if (MODE == TM_RANDOM) {
+        f[i] = (VT)random_start(i - s.start);
+      } else if (MODE == TM_SELECT) {
+        if (!s.warm) f[i] = V[i];
       } else if (MODE == TM_RESID1) {
         double fi = (double)f[i];
         ll sl = i >> 5;
@@ -1406,18 +1438,14 @@ __global__ void k_set_active(GState *__restrict__ gs, int ngroups) {
   }
 }
 
+__global__ void k_set_warm(GState *__restrict__ gs, int ngroups, const int *__restrict__ use) {
+  int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < ngroups) gs[g].warm = use[g];
+}
+
 // ----------------------------------------------------------------------------
 // Host-side segmented Lanczos engine
 // ----------------------------------------------------------------------------
-struct Level {
-  DBuf<unsigned> ell;
-  DBuf<ll> slice_off;
-  DBuf<int> slice_w;
-  ll nnz = 0;    // restricted nonzeros of the active rows
-  ll rows = 0;   // active rows
-  int max_w = 0; // widest slice
-};
-
 template <typename VT>
 struct Lanczos {
   int A = 0;      // groups
@@ -1447,6 +1475,7 @@ struct Lanczos {
   // the same choice for the SpMV (PARRSB_GPU_SPMV_FUSED=1: fused)
   bool sp_fused = false;
   int ritz_bd = 256;             // threads per block of k_ritz
+  bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
 
   void setup(const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N_, int miter) {
@@ -1530,12 +1559,14 @@ struct Lanczos {
     return fa;
   }
 
+  // y_in / v_in replace the y64 and V arguments (TM_LOAD_Y, TM_SELECT)
   template <int MODE, int GATE, int FUSE = -1>
-  void tile(int it = 0, const Level *lv = nullptr, double tol = 0.0, int mpass = 0) {
+  void tile(int it = 0, const Level *lv = nullptr, double tol = 0.0, int mpass = 0,
+            const double *y_in = nullptr, VT *v_in = nullptr) {
     launch_pdl(k_tile<VT, MODE, GATE, FUSE>, T, bd, 0, ctx().stream, tbeg.p, tend.p, tgrp.p,
-               gs.p, f.p, V.p, N, it, part.p, lv ? lv->ell.p : nullptr,
-               lv ? lv->slice_off.p : nullptr, lv ? lv->slice_w.p : nullptr, y64.p,
-               fargs(it, tol, mpass));
+               gs.p, f.p, v_in ? v_in : V.p, N, it, part.p, lv ? lv->ell.p : nullptr,
+               lv ? lv->slice_off.p : nullptr, lv ? lv->slice_w.p : nullptr,
+               y_in ? const_cast<double *>(y_in) : y64.p, fargs(it, tol, mpass));
   }
   template <int OP, int GATE>
   void fin(int it = 0, double tol = 0.0, int mpass = 0) {
@@ -1549,6 +1580,61 @@ struct Lanczos {
     tile<TM_IV_SQ, GATE_ALL>();
     fin<FIN_IV_NORM, GATE_ALL>();
     tile<TM_IV_WRITE, GATE_ALL>();
+  }
+
+  // Seeded random start (uniform in [-1, 1) per position of a group); the
+  // first pass removes its mean and normalises it.
+  void random_vector() { tile<TM_RANDOM, GATE_ALL>(); }
+
+  // Start vectors with a learned candidate y (FP64 per position): every
+  // group starts from y or from the fallback start (start_kind 0: the
+  // reference's step vector, 1: random), whichever has the lower FP64
+  // eigen-residual ||L f - rho f|| / ||f|| (the judge).  Groups smaller
+  // than warm_min keep the fallback.  Leaves the start in f.
+  void choose_start(const Level &lv, const double *y, int start_kind, ll warm_min) {
+    cudaStream_t st = ctx().stream;
+    k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
+    CK_LAUNCH();
+    if (start_kind == 1) random_vector(); else initial_vector();
+    residual(lv);
+    download(hgs);
+    std::vector<double> r_fb(A);
+    for (int g = 0; g < A; g++) r_fb[g] = hgs[g].resid;
+    CK(cudaMemcpyAsync(p.p, f.p, (size_t)N * sizeof(VT), cudaMemcpyDeviceToDevice, st));
+    tile<TM_LOAD_Y, GATE_ALL>(0, nullptr, 0.0, 0, y);
+    tile<TM_SUM_F, GATE_ALL>();
+    fin<FIN_RITZ_MEAN, GATE_ALL>();
+    tile<TM_SUB_C, GATE_ALL>();
+    residual(lv);
+    download(hgs);
+    parrsb_stats &S = ctx().stats;
+    double lf = 0.0, lw = 0.0;
+    long long tried = 0;
+    std::vector<int> use(A, 0);
+    for (int g = 0; g < A; g++) {
+      if (hgs[g].n < warm_min) continue;
+      const double rw = hgs[g].resid;
+      tried++;
+      lf += log10(std::max(r_fb[g], 1e-300));
+      lw += log10(std::max(rw, 1e-300));
+      use[g] = rw < r_fb[g] ? 1 : 0;  // NaN never wins
+      S.warm_used += use[g];
+    }
+    // running geometric means over every judged group of the call
+    const long long t0 = S.warm_tried;
+    if (tried > 0) {
+      const double pf = t0 ? log10(S.start_resid_fallback) * t0 : 0.0;
+      const double pw = t0 ? log10(S.start_resid_warm) * t0 : 0.0;
+      S.start_resid_fallback = pow(10.0, (pf + lf) / (double)(t0 + tried));
+      S.start_resid_warm = pow(10.0, (pw + lw) / (double)(t0 + tried));
+      S.warm_tried = t0 + tried;
+    }
+    DBuf<int> du(A);
+    h2d(du.p, use.data(), A);
+    k_set_warm<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A, du.p);
+    CK_LAUNCH();
+    tile<TM_SELECT, GATE_ALL>(0, nullptr, 0.0, 0, nullptr, p.p);
+    sync();
   }
 
   // One Lanczos pass (restart) for the active groups: the body that the
@@ -1607,7 +1693,16 @@ struct Lanczos {
     mark(4 * MI + 5);
     fin<FIN_RITZ_MEAN, GATE_ACTIVE>();
     tile<TM_SUB_C, GATE_ACTIVE>();
-    fin<FIN_PASS_END, GATE_ACTIVE>(0, tol, mpass);
+    if (!resid_stop) {
+      fin<FIN_PASS_END, GATE_ACTIVE>(0, tol, mpass);
+    } else {
+      // restart until the Ritz vector's FP64 eigen-residual is at most tol
+      fin<FIN_PASS_END_R, GATE_ACTIVE>(0, tol, mpass);
+      tile<TM_RESID1, GATE_ACTIVE>(0, &lv);
+      fin<FIN_RESID1, GATE_ACTIVE>();
+      tile<TM_RESID2, GATE_ACTIVE>(0, &lv);
+      fin<FIN_RESID_GATE, GATE_ACTIVE>(0, tol, mpass);
+    }
   }
 
   // shared memory of one k_spmv_tma stage (nw slices of the widest width)
@@ -1686,8 +1781,12 @@ struct Lanczos {
   }
 
   // Runs all passes; f holds the normalised Fiedler vectors afterwards.
-  void run(const Level &lv, double tol, int mpass, bool use_graph, bool warm) {
+  // warm: f already holds the start vectors; otherwise start_kind selects
+  // the reference's step vector (0) or a random one (1).
+  void run(const Level &lv, double tol, int mpass, bool use_graph, bool warm,
+           int start_kind = 0) {
     cudaStream_t st = ctx().stream;
+    if (resid_stop) y64.ensure((size_t)N);
     // the vectors are scratch until the first pass initialises them
     CK(cudaMemsetAsync(p.p, 0, (size_t)N * sizeof(VT), st));
     if (eig_smem() > 48 * 1024)
@@ -1696,7 +1795,12 @@ struct Lanczos {
     autotune(lv);
     k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
     CK_LAUNCH();
-    if (!warm) initial_vector();
+    if (!warm) {
+      if (start_kind == 1)
+        random_vector();
+      else
+        initial_vector();
+    }
     long long launches = 0;
     cudaGraphExec_t exec = nullptr;
     cudaGraph_t graph = nullptr;
@@ -1714,7 +1818,8 @@ struct Lanczos {
       CK(cudaStreamEndCapture(st, &graph));
       CK(cudaGraphInstantiate(&exec, graph, 0));
     }
-    const long long per_pass_kernels = 4 + (long long)MI * 3 + 5;
+    const long long per_pass_kernels =
+        4 + (long long)MI * (pr_fused ? 3 : 5) + (sp_fused ? 0 : MI) + 5 + (resid_stop ? 4 : 0);
     launches = 0;
     // PARRSB_GPU_LEVEL_LOG=1 (timing mode): one line per level on stderr
     const bool level_log = !ev.empty() && getenv("PARRSB_GPU_LEVEL_LOG");
@@ -2153,14 +2258,19 @@ std::vector<int> count_components_level(const Level &lv, const int *half, ll N,
   return hc;
 }
 
+// y_warm (optional): learned start candidates per position (FP64), judged
+// per group against the fallback start before Lanczos runs.
 template <typename VT>
 void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
                        const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N,
-                       double *f_pos, std::vector<GState> &res) {
+                       double *f_pos, std::vector<GState> &res,
+                       const double *y_warm = nullptr) {
   lz.setup(gstart, gn, N, o.miter);
+  lz.resid_stop = o.resid_stop != 0;
   {
     StageTimer tm(PARRSB_STAGE_LANCZOS);
-    lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, false);
+    if (y_warm) lz.choose_start(lv, y_warm, o.start, o.warm_min);
+    lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, y_warm != nullptr, o.start);
   }
   if (o.check_resid) lz.residual(lv);
   k_to_double<VT><<<grid_for(N, 256), 256, 0, ctx().stream>>>(lz.f.p, N, f_pos);
@@ -2248,7 +2358,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
                    "dual-graph weight >= 16 or more than 2^28 elements"};
   DBuf<int> perm((size_t)N), inv((size_t)N), grp((size_t)N), half((size_t)N),
       segpos((size_t)N), idx((size_t)N), moved((size_t)N), flag((size_t)N);
-  DBuf<double> f_pos((size_t)N), f_tmp((size_t)N);
+  DBuf<double> f_pos((size_t)N), f_tmp((size_t)N), y_pred;
   DBuf<u64> keys((size_t)N);
   DBuf<int> vals((size_t)N), perm2((size_t)N);
   std::vector<HGroup> groups;
@@ -2320,10 +2430,35 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
       CK_LAUNCH();
       build_level(G, perm.p, inv.p, grp.p, N, lv);
     }
+    // ---- learned warm start: predictions for the groups of this level
+    // that are large enough (the judge in Lanczos::choose_start decides)
+    const double *y_warm = nullptr;
+    if (o.warm && nv == 8) {
+      ll biggest = 0;
+      for (int g = 0; g < na; g++) biggest = std::max(biggest, an[g]);
+      if (biggest >= std::max<ll>(o.warm_min, 2)) {
+        if (!warm_net_ready())
+          throw ArgError{PARRSB_ERR_ARGS, "warm start requested but no network installed"};
+        cudaEvent_t w0, w1;
+        CK(cudaEventCreate(&w0));
+        CK(cudaEventCreate(&w1));
+        CK(cudaEventRecord(w0, st));
+        y_pred.ensure((size_t)N);
+        warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
+        CK(cudaEventRecord(w1, st));
+        CK(cudaEventSynchronize(w1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, w0, w1));
+        S.warm_ms += ms;
+        cudaEventDestroy(w0);
+        cudaEventDestroy(w1);
+        y_warm = y_pred.p;
+      }
+    }
     // ---- Fiedler vectors (src/rsb.c:300-302)
     std::vector<GState> res;
     if (o.batched) {
-      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res);
+      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res, y_warm);
     } else {
       // plain path: every group of the level solved by its own launches
       RsbOpts o1 = o;
@@ -2331,7 +2466,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
       for (int g = 0; g < na; g++) {
         std::vector<GState> r1;
         std::vector<ll> s1 = {ast[g]}, n1 = {an[g]};
-        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1);
+        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1, y_warm);
         CK(cudaMemcpyAsync(f_pos.p + ast[g], f_tmp.p + ast[g], an[g] * sizeof(double),
                            cudaMemcpyDeviceToDevice, st));
         res.push_back(r1[0]);
@@ -2667,42 +2802,54 @@ void iota_device(int *d, ll N) {
   CK_LAUNCH();
 }
 
-void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_of, int ngroups,
-                       int *counts) {
+void build_group_level(const long long *d_vtx, ll N, int nv, const int *d_group_of,
+                       int ngroups, GroupLevel &out) {
   cudaStream_t st = ctx().stream;
-  for (int g = 0; g < ngroups; g++) counts[g] = 0;
+  out.N = N;
+  out.gstart.assign(ngroups, 0);
+  out.gn.assign(ngroups, 0);
   if (N == 0) return;
   SortWs sws;
   Graph G;
   build_dual_graph(d_vtx, N, nv, G, sws);
-  if (N >= (1ll << 28))
-    throw ArgError{PARRSB_ERR_UNSUPPORTED, "more than 2^28 elements"};
+  if (G.max_w >= 16 || N >= (1ll << 28))
+    throw ArgError{PARRSB_ERR_UNSUPPORTED, "dual-graph weight >= 16 or more than 2^28 elements"};
   DBuf<u64> keys((size_t)N);
-  DBuf<int> perm((size_t)N), cnt((size_t)ngroups), inv((size_t)N), grp((size_t)N);
+  DBuf<int> cnt((size_t)ngroups), inv((size_t)N);
+  out.perm.ensure((size_t)N), out.grp.ensure((size_t)N);
   CK(cudaMemsetAsync(cnt.p, 0, (size_t)ngroups * sizeof(int), st));
-  k_group_keys_opt<<<grid_for(N, 256), 256, 0, st>>>(d_group_of, N, ngroups, keys.p, perm.p,
+  k_group_keys_opt<<<grid_for(N, 256), 256, 0, st>>>(d_group_of, N, ngroups, keys.p, out.perm.p,
                                                      cnt.p);
   CK_LAUNCH();
-  seg_sort_pairs(keys, perm, N, nullptr, 1, sws);
+  seg_sort_pairs(keys, out.perm, N, nullptr, 1, sws);
   std::vector<int> hc(ngroups);
   d2h(hc.data(), cnt.p, ngroups);
   sync();
-  std::vector<ll> st_, n_, hstart(ngroups, 0);
+  std::vector<ll> st_, n_;
   std::vector<int> id_;
   ll pos = 0;
   for (int g = 0; g < ngroups; g++) {
+    out.gstart[g] = pos, out.gn[g] = hc[g];
     st_.push_back(pos), n_.push_back(hc[g]), id_.push_back(g);
-    hstart[g] = hc[g] ? pos : 0;  // any valid row for an empty group (never consulted)
     pos += hc[g];
   }
-  CK(cudaMemsetAsync(grp.p, 0xff, (size_t)N * sizeof(int), st));  // no group: -1
-  fill_groups(st_, n_, id_, grp.p, N);
-  k_inv_perm<<<grid_for(N, 256), 256, 0, st>>>(perm.p, N, inv.p);
+  CK(cudaMemsetAsync(out.grp.p, 0xff, (size_t)N * sizeof(int), st));  // no group: -1
+  fill_groups(st_, n_, id_, out.grp.p, N);
+  k_inv_perm<<<grid_for(N, 256), 256, 0, st>>>(out.perm.p, N, inv.p);
   CK_LAUNCH();
-  Level lv;
-  build_level(G, perm.p, inv.p, grp.p, N, lv);
-  std::vector<int> c = count_components_level(lv, grp.p, N, hstart);
-  for (int g = 0; g < ngroups; g++) counts[g] = hc[g] ? c[g] : 0;
+  build_level(G, out.perm.p, inv.p, out.grp.p, N, out.lv);
+}
+
+void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_of, int ngroups,
+                       int *counts) {
+  for (int g = 0; g < ngroups; g++) counts[g] = 0;
+  if (N == 0) return;
+  GroupLevel gl;
+  build_group_level(d_vtx, N, nv, d_group_of, ngroups, gl);
+  std::vector<ll> hstart(ngroups, 0);
+  for (int g = 0; g < ngroups; g++) hstart[g] = gl.gn[g] ? gl.gstart[g] : 0;  // any valid row
+  std::vector<int> c = count_components_level(gl.lv, gl.grp.p, N, hstart);
+  for (int g = 0; g < ngroups; g++) counts[g] = gl.gn[g] ? c[g] : 0;
 }
 
 void dual_graph_device(const long long *d_vtx, ll N, int nv, std::vector<ll> &rowptr,

@@ -18,6 +18,20 @@ struct Graph {
 void build_dual_graph(const long long *d_vtx, ll nel, int nv, Graph &g,
                       SortWs &sws);
 
+// A level's graph: the dual graph restricted to the current groups and
+// re-indexed into the current element order, as sliced ELL (slices of 32
+// consecutive rows, column-major inside a slice, one packed uint32 per
+// entry: column in bits 0-27, weight in bits 28-31; padding entries have
+// weight 0).
+struct Level {
+  DBuf<unsigned> ell;
+  DBuf<ll> slice_off;
+  DBuf<int> slice_w;
+  ll nnz = 0;    // restricted nonzeros of the active rows
+  ll rows = 0;   // active rows
+  int max_w = 0; // widest slice
+};
+
 struct RsbOpts {
   int pre = 1;          // 0 none, 1 RCB, 2 RIB
   int miter = 50;
@@ -29,6 +43,19 @@ struct RsbOpts {
   int profile = 0;
   int use_graphs = 1;   // capture each Lanczos pass in a CUDA graph
   int batched = 1;      // all groups of a level per launch (0: one group at a time)
+  // Start vector of every Lanczos run: 0 the reference's step vector
+  // (src/fiedler.c:574-578), 1 a seeded random vector.  With warm != 0 the
+  // learned warm start is judged against it per group (lower FP64
+  // eigen-residual wins) for groups of at least warm_min elements.
+  int start = 0;
+  int warm = 0;
+  ll warm_min = 0;
+  // Stopping rule: 0 the reference's (a restart ends when the CG residual
+  // falls below tol times its start, src/fiedler.c:448,500, or after miter
+  // steps; Lanczos ends after a restart that needed fewer than miter steps);
+  // 1 also restart until the Ritz vector's FP64 eigen-residual
+  // ||L f - rho f|| / ||f|| is at most tol (or mpass restarts).
+  int resid_stop = 0;
 };
 
 // Starting point of a recursion other than one group of all elements:
@@ -57,6 +84,20 @@ void fiedler_groups_device(const long long *d_vtx, ll N, int nv,
                            const int *d_group_of, int ngroups,
                            const RsbOpts &o, double *d_f, long long *iters,
                            double *resid);
+
+// Elements of groups given per element (group_of[e] in [0, ngroups), or < 0
+// for none), ordered by group (stable: element order inside a group), with
+// the level graph of the groups: perm[i] = element at position i, grp[i] =
+// its group (-1 after the grouped elements), group g at positions
+// [gstart[g], gstart[g] + gn[g]).
+struct GroupLevel {
+  DBuf<int> perm, grp;
+  std::vector<ll> gstart, gn;
+  Level lv;
+  ll N = 0;
+};
+void build_group_level(const long long *d_vtx, ll N, int nv, const int *d_group_of,
+                       int ngroups, GroupLevel &out);
 
 // Vertex-connected components of each group (group_of[e] < 0: no group);
 // counts (host, ngroups) receives the number per group.

@@ -1,0 +1,163 @@
+"""The learned warm start on the GPU, through the C ABI:
+
+- input features against the FP64 restatement (oracle/warm_oracle.py);
+- forward pass and every parameter's gradient against the FP64 forward and
+  backward run on the GPU's own features with the same BF16-rounded
+  weights (tolerances: BF16 activations, 8 significant bits);
+- Adam steps of the library's kernels lower the loss;
+- RSB with the warm start (judged per group) keeps the oracle's part sizes
+  and a cut within 1%, and the residual-stop mode meets
+  ||L f - rho f|| / ||f|| <= rsb_tol for every bisection;
+- the shipped network's gain over the method without it: its start vectors
+  have far lower eigen-residuals than the reference's step vector.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import parrsb_gb300 as P
+from parrsb_gb300 import meshgen
+from parrsb_gb300 import warm as Wm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu(lib):
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+    yield
+    P.finalize()
+
+
+def _small_set(seed=3, count=6):
+    return Wm.training_meshes(count, seed=seed, smin=300, smax=3000)
+
+
+def _graph(vtx, group):
+    from oracle import oracle as O
+    from oracle import warm_oracle as W
+    rp, col, w = O.dual_graph(vtx)
+    return W.restrict(rp, col, w, group)
+
+
+def test_features_match_restatement():
+    import torch
+    from oracle import oracle as O
+    from oracle import warm_oracle as W
+    vtx, xyz, group = _small_set()
+    b = Wm.Batch(vtx, xyz, group, int(group.max()) + 1)
+    X = b.features().cpu().numpy().astype(np.float64)
+    b.close()
+    rows, col, w = _graph(vtx, group)
+    Xo = W.features(O.centroids(xyz, 8), group.astype(np.int64), rows, w)
+    # BF16 features: 8 significant bits
+    np.testing.assert_allclose(X[:, :4], Xo[:, :4], rtol=2 ** -7, atol=2 ** -7)
+    assert np.all(X[:, 4:] == 0)
+
+
+def _gpu_step(b, params, label):
+    import torch
+    d_p = torch.from_numpy(params.astype(np.float32)).cuda()
+    d_l = torch.from_numpy(label).cuda()
+    d_g = torch.zeros_like(d_p)
+    loss, pred = b.step(d_p, d_l, d_g, want_pred=True)
+    return loss, pred.cpu().numpy().astype(np.float64), d_g.cpu().numpy().astype(np.float64)
+
+
+def test_forward_and_gradient_match_fp64_restatement():
+    from oracle import warm_oracle as W
+    vtx, xyz, group = _small_set(seed=4, count=5)
+    G = int(group.max()) + 1
+    b = Wm.Batch(vtx, xyz, group, G)
+    X = b.features().cpu().numpy().astype(np.float64)
+    rows, col, w = _graph(vtx, group)
+    rng = np.random.default_rng(7)
+    params = Wm.init_params(11).astype(np.float64)
+    params[W.OFF["b1"][0]:W.OFF["b1"][1]] = rng.normal(0, 0.1, 64)
+    label = np.ascontiguousarray(np.cos(np.pi * X[:, 0] * 0.5) + 0.1 * rng.normal(size=len(X)))
+    loss, pred, grad = _gpu_step(b, params, label)
+    b.close()
+    y, _ = W.forward(X, rows, col, w, params.astype(np.float32).astype(np.float64))
+    Lo, go = W.gradient(X, rows, col, w, params.astype(np.float32).astype(np.float64), label,
+                        group.astype(np.int64))
+    # prediction: BF16 activations through three layers
+    assert np.linalg.norm(pred - y) <= 3e-2 * np.linalg.norm(y)
+    assert abs(loss - Lo) <= 2e-2 * max(Lo, 1e-3) + 1e-4
+    for name, (a, z) in W.OFF.items():
+        ga, gb = grad[a:z], go[a:z]
+        nrm = np.linalg.norm(gb)
+        assert np.linalg.norm(ga - gb) <= 6e-2 * nrm + 1e-6, (name, np.linalg.norm(ga - gb), nrm)
+        if nrm > 1e-6 and z - a > 1:
+            assert ga @ gb / (np.linalg.norm(ga) * nrm) > 0.995, name
+
+
+def test_adam_steps_lower_the_loss():
+    import torch
+    vtx, xyz, group = _small_set(seed=5, count=8)
+    G = int(group.max()) + 1
+    f, _, _ = Wm.label(vtx, group, G)
+    b = Wm.Batch(vtx, xyz, group, G)
+    p = torch.from_numpy(Wm.init_params(2)).cuda()
+    m, v, g = torch.zeros_like(p), torch.zeros_like(p), torch.zeros_like(p)
+    lab = torch.from_numpy(f).cuda()
+    first, _ = b.step(p, lab, g)
+    for step in range(1, 61):
+        b.step(p, lab, g)
+        Wm.adam(p, m, v, g, step, 3e-3)
+    last, _ = b.step(p, lab, g)
+    b.close()
+    assert last < 0.5 * first, (first, last)
+
+
+def _rsb(vtx, xyz, nparts, monkeypatch, **env):
+    for k, val in env.items():
+        monkeypatch.setenv(k, str(val))
+    part = P.part_mesh(vtx, xyz, nparts, partitioner=0)
+    return part, P.last_stats()
+
+
+def test_rsb_warm_start_keeps_partition_quality(oracle, monkeypatch):
+    Wm.install(Wm.init_params(0) if not os.path.exists(Wm.WEIGHTS) else None)
+    vtx, xyz = meshgen.box_hex(40, 32, 20, jitter=0.1, seed=8)
+    part, st = _rsb(vtx, xyz, 8, monkeypatch, PARRSB_GPU_WARM=1)
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, 8, partitioner=0)
+    np.testing.assert_array_equal(np.bincount(part, minlength=8), np.bincount(ref, minlength=8))
+    q, qr = oracle.part_quality(part, vtx, 8), oracle.part_quality(ref, vtx, 8)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+    assert st.warm_tried == 7 and st.unconverged == 0
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+def test_residual_stop_meets_tolerance(oracle, monkeypatch, fp32):
+    """With PARRSB_GPU_RESID_STOP=1 every bisection restarts until its Ritz
+    vector's FP64 eigen-residual is at most rsb_tol (1e-5); the reference's
+    rule alone leaves 2.3e-5 on this machine."""
+    vtx, xyz = meshgen.box_hex(16, 16, 16, jitter=0.1, seed=0)
+    part, st = _rsb(vtx, xyz, 8, monkeypatch, PARRSB_GPU_RESID_STOP=1, PARRSB_GPU_FP32=fp32)
+    assert st.max_fiedler_resid <= 1e-5
+    assert st.unconverged == 0
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, 8, partitioner=0)
+    np.testing.assert_array_equal(np.bincount(part, minlength=8), np.bincount(ref, minlength=8))
+    q, qr = oracle.part_quality(part, vtx, 8), oracle.part_quality(ref, vtx, 8)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
+
+
+@pytest.mark.skipif(not os.path.exists(Wm.WEIGHTS), reason="no trained network shipped")
+def test_trained_network_gain(monkeypatch):
+    """What the shipped network gains over the method without it, on meshes
+    it was not trained on: the judged start residuals, the share of groups
+    that start from it, and the Lanczos steps with and without it."""
+    Wm.install()
+    vtx, xyz = meshgen.box_hex(72, 48, 36, jitter=0.1, seed=123)
+    _, cold = _rsb(vtx, xyz, 16, monkeypatch, PARRSB_GPU_WARM=0)
+    cold_steps = cold.lanczos_iters
+    _, hot = _rsb(vtx, xyz, 16, monkeypatch, PARRSB_GPU_WARM=1)
+    assert hot.warm_tried == 15
+    assert hot.warm_used >= 12
+    assert hot.start_resid_warm < 0.1 * hot.start_resid_fallback
+    print(f"steps cold {cold_steps} warm {hot.lanczos_iters}; start residual "
+          f"{hot.start_resid_fallback:.3e} -> {hot.start_resid_warm:.3e}")
