@@ -345,7 +345,14 @@ def main():
     os.environ.setdefault("PARRSB_VERBOSE_LEVEL", "0")
     import parrsb_gb300 as P
     from parrsb_gb300 import meshgen
+    from parrsb_gb300 import warm as W
     from parrsb_gb300.options import ParrsbOptions
+
+    # the shipped warm-start network, read by the library when a call asks
+    # for the learned start (PARRSB_GPU_WARM=1)
+    warm_ok = os.path.exists(W.WEIGHTS)
+    if warm_ok:
+        os.environ.setdefault("PARRSB_GPU_WARM_WEIGHTS", W.WEIGHTS)
 
     shape = tuple(int(x) for x in args.shape.split(",")) if args.shape else SHAPE
     nparts = args.nparts or NPARTS
@@ -453,6 +460,49 @@ def main():
         os.environ["PARRSB_GPU_BATCHED"] = "1"
 
     # ---- the same step with FP64 vectors: time and the error of the mixed path
+    # ---- start vectors and stopping rules, one step each on the same mesh:
+    # the reference's step start, the learned start (judged per group), a
+    # random start; the reference's stopping rule, and restarts until the
+    # eigen-residual is at most rsb_tol
+    starts = None
+    if not args.no_plain:
+        starts = {}
+        legs = [("reference_start", {}), ("random_start", {"PARRSB_GPU_START": "1"}),
+                ("geometric_start", {"PARRSB_GPU_START": "2"}),
+                ("reference_start_resid_stop", {"PARRSB_GPU_RESID_STOP": "1"})]
+        if warm_ok:
+            legs += [("warm_start", {"PARRSB_GPU_WARM": "1"}),
+                     ("warm_start_resid_stop", {"PARRSB_GPU_WARM": "1",
+                                                "PARRSB_GPU_RESID_STOP": "1"})]
+        for name, env in legs:
+            saved = {k: os.environ.get(k) for k in env}
+            os.environ.update(env)
+            try:
+                step_device()  # warm-up of this leg's kernels and graphs
+                barrier()
+                ta, tb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ta.record()
+                sl = step_device()
+                tb.record()
+                barrier()
+                ql = P.part_quality(d_part.cpu().numpy(), vtx, nparts)
+                starts[name] = {
+                    "s": max_over_ranks(ta.elapsed_time(tb) / 1e3),
+                    "lanczos_steps": int(sl.lanczos_iters), "passes": int(sl.lanczos_passes),
+                    "weighted_cut": ql[0], "imbalance": ql[5],
+                    "max_fiedler_resid": sl.max_fiedler_resid,
+                    "unconverged": int(sl.unconverged),
+                    "warm_groups": [int(sl.warm_used), int(sl.warm_tried)],
+                    "warm_inference_ms": round(sl.warm_ms, 2),
+                    "start_resid": [sl.start_resid_fallback, sl.start_resid_warm],
+                    "level_steps": [int(x) for x in sl.level_steps[:int(sl.levels)]]}
+            finally:
+                for k, v in saved.items():
+                    if v is None:
+                        os.environ.pop(k, None)
+                    else:
+                        os.environ[k] = v
+
     fp64 = None
     if not args.no_plain and os.environ["PARRSB_GPU_FP32"] == "1":
         os.environ["PARRSB_GPU_FP32"] = "0"
@@ -531,6 +581,7 @@ def main():
                      "algorithmic_bytes_per_launch": per_launch_bytes},
         "cpu_baseline": cpu,
         "plain_gpu": plain,
+        "start_vectors": starts,
         "fp64_gpu": fp64,
         "other_rows": extras,
         "clocks": clock_info,

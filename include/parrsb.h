@@ -169,6 +169,7 @@ typedef struct {
   double warm_ms;             /* warm-start network inference (all levels) */
   double start_resid_fallback;/* geometric mean of the judged groups' start */
   double start_resid_warm;    /*   residuals: fallback and learned starts */
+  long long level_steps[16];  /* Lanczos steps per bisection level (last: 15+) */
 } parrsb_stats;
 
 enum {

@@ -62,13 +62,14 @@ class Stats(ctypes.Structure):
                 ("warm_used", ctypes.c_longlong),
                 ("warm_ms", ctypes.c_double),
                 ("start_resid_fallback", ctypes.c_double),
-                ("start_resid_warm", ctypes.c_double)]
+                ("start_resid_warm", ctypes.c_double),
+                ("level_steps", ctypes.c_longlong * 16)]
 
     def as_dict(self):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            d[name] = list(v) if name in ("stage_ms", "lanczos_ms") else v
+            d[name] = list(v) if name in ("stage_ms", "lanczos_ms", "level_steps") else v
         return d
 
 

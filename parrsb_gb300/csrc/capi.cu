@@ -601,6 +601,8 @@ extern "C" int parrsb_fiedler_groups(double *fiedler, long long *iters, double *
       ro.fp32 = env_int("PARRSB_GPU_FP32", 0);
       ro.use_graphs = env_int("PARRSB_GPU_GRAPHS", 1);
       ro.batched = batched ? 1 : 0;
+      ro.start = env_int("PARRSB_GPU_START", 0);
+      ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
       fiedler_groups_device(dv.p, N, nv, dg.p, ngroups, ro, df.p, it.data(), rs.data());
       d2h(fiedler, df.p, (size_t)N);
       sync();

@@ -2433,18 +2433,21 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     // ---- learned warm start: predictions for the groups of this level
     // that are large enough (the judge in Lanczos::choose_start decides)
     const double *y_warm = nullptr;
-    if (o.warm && nv == 8) {
+    if ((o.warm || o.start == 2) && nv == 8) {
       ll biggest = 0;
       for (int g = 0; g < na; g++) biggest = std::max(biggest, an[g]);
       if (biggest >= std::max<ll>(o.warm_min, 2)) {
-        if (!warm_net_ready())
+        if (o.warm && !warm_net_ready())
           throw ArgError{PARRSB_ERR_ARGS, "warm start requested but no network installed"};
         cudaEvent_t w0, w1;
         CK(cudaEventCreate(&w0));
         CK(cudaEventCreate(&w1));
         CK(cudaEventRecord(w0, st));
         y_pred.ensure((size_t)N);
-        warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
+        if (o.warm)
+          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
+        else  // start 2: the geometric start in place of the network
+          geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;
@@ -2474,6 +2477,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     }
     ll rows = 0;
     for (int g = 0; g < na; g++) {
+      S.level_steps[std::min(cut, 15)] += res[g].total_iters;
       S.lanczos_iters += res[g].total_iters;
       S.lanczos_row_iters += res[g].total_iters * res[g].n;
       rows += res[g].n;

@@ -267,13 +267,16 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
 }
 
 // Input features of every position: X[i] = (x~ (3), deg / 56, 0, 0, 0, 0)
-// in BF16; rows outside the groups (grp < 0) and padding rows are zero.
+// in FP32 (the first layer multiplies them as a pair of BF16 values, high
+// and low part, so positions keep about 16 significant bits: a group may
+// be thousands of elements long); rows outside the groups (grp < 0) and
+// padding rows are zero.
 // wsum[i] = sum_j w_ij in the level graph (FP32, reused by the backward).
 __global__ void k_mp_features(const int *__restrict__ perm, const int *__restrict__ grp,
                               const double *__restrict__ cent, ll nel,
                               const double *__restrict__ frame, const unsigned *__restrict__ ell,
                               const ll *__restrict__ slice_off, const int *__restrict__ slice_w,
-                              ll N, ll Npad, bf16 *__restrict__ X, float *__restrict__ wsum) {
+                              ll N, ll Npad, float *__restrict__ X, float *__restrict__ wsum) {
   const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Npad) return;
   float v[MP_FIN] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -293,10 +296,9 @@ __global__ void k_mp_features(const int *__restrict__ perm, const int *__restric
     ws = (float)acc;
     v[3] = (float)((double)acc * MP_DEG_SCALE);
   }
-  __align__(16) bf16 o[MP_FIN];
-#pragma unroll
-  for (int k = 0; k < MP_FIN; k++) o[k] = __float2bfloat16_rn(v[k]);
-  *reinterpret_cast<uint4 *>(X + i * MP_FIN) = *reinterpret_cast<const uint4 *>(o);
+  float4 *o = reinterpret_cast<float4 *>(X + i * MP_FIN);
+  o[0] = make_float4(v[0], v[1], v[2], v[3]);
+  o[1] = make_float4(v[4], v[5], v[6], v[7]);
   if (wsum) wsum[i] = ws;
 }
 
@@ -345,15 +347,20 @@ __device__ __forceinline__ void gather_mean(const bf16 *__restrict__ H, const un
 //   Z = A W + b (tensor cores, FP32), h = relu(Z) -> Hout (BF16)
 // AG (optional): the neighbour means, kept for the backward pass.
 // HEAD: also y = h . wo + bo (FP32) per row.
-template <int DIN, bool HEAD>
+// F32IN (first layer): inputs and neighbour means in FP32, split into a
+// high and a low BF16 part; Z = A_hi W + A_lo W (two MMAs), AG in FP32.
+template <int DIN, bool HEAD, bool F32IN = false>
 __global__ void __launch_bounds__(MP_THREADS)
-k_mp_fwd(const bf16 *__restrict__ Hin, const unsigned *__restrict__ ell,
+k_mp_fwd(const void *__restrict__ Hin_, const unsigned *__restrict__ ell,
          const ll *__restrict__ slice_off, const int *__restrict__ slice_w,
          const float *__restrict__ wsum, ll N, ll Npad, const bf16 *__restrict__ Wf,
-         const float *__restrict__ bias, bf16 *__restrict__ Hout, bf16 *__restrict__ AG,
+         const float *__restrict__ bias, bf16 *__restrict__ Hout, void *__restrict__ AG_,
          const float *__restrict__ wo, const float *__restrict__ bo, float *__restrict__ y) {
   constexpr int K = 2 * DIN, KP = K + 8;
+  const bf16 *__restrict__ Hin = static_cast<const bf16 *>(Hin_);
+  bf16 *__restrict__ AG = static_cast<bf16 *>(AG_);
   __shared__ __align__(16) bf16 sA[MP_ROWS * KP];
+  __shared__ __align__(16) bf16 sAlo[F32IN ? MP_ROWS * KP : 8];
   __shared__ __align__(16) bf16 sW[MP_HID * KP];
   for (int q = threadIdx.x; q < MP_HID * (K / 8); q += blockDim.x) {
     const int n = q / (K / 8), k8 = q % (K / 8);
@@ -368,6 +375,52 @@ k_mp_fwd(const bf16 *__restrict__ Hin, const unsigned *__restrict__ ell,
   for (ll tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const ll base = tile * MP_ROWS;
     __syncthreads();  // sA is free again (and sW is loaded)
+    if (F32IN) {  // one thread per row, 8 FP32 features
+      const float *Hf = static_cast<const float *>(Hin_);
+      float *AGf = static_cast<float *>(AG_);
+      for (int r = threadIdx.x; r < MP_ROWS; r += MP_THREADS) {
+        const ll i = base + r;
+        float sv[8] = {0, 0, 0, 0, 0, 0, 0, 0}, acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (i < N) {
+          const float4 a = reinterpret_cast<const float4 *>(Hf + i * 8)[0];
+          const float4 b = reinterpret_cast<const float4 *>(Hf + i * 8)[1];
+          sv[0] = a.x, sv[1] = a.y, sv[2] = a.z, sv[3] = a.w;
+          sv[4] = b.x, sv[5] = b.y, sv[6] = b.z, sv[7] = b.w;
+          const ll sl = i >> 5;
+          const unsigned *ep = ell + slice_off[sl] + (i & 31);
+          const int wd = slice_w[sl];
+          for (int k = 0; k < wd; k++) {
+            const unsigned x = ep[(ll)k * 32];
+            const unsigned w = x >> 28;
+            if (!w) continue;
+            const ll j = x & 0x0FFFFFFFu;
+            const float4 c = reinterpret_cast<const float4 *>(Hf + j * 8)[0];
+            const float4 d = reinterpret_cast<const float4 *>(Hf + j * 8)[1];
+            const float fw = (float)w;
+            acc[0] = fmaf(fw, c.x, acc[0]), acc[1] = fmaf(fw, c.y, acc[1]);
+            acc[2] = fmaf(fw, c.z, acc[2]), acc[3] = fmaf(fw, c.w, acc[3]);
+            acc[4] = fmaf(fw, d.x, acc[4]), acc[5] = fmaf(fw, d.y, acc[5]);
+            acc[6] = fmaf(fw, d.z, acc[6]), acc[7] = fmaf(fw, d.w, acc[7]);
+          }
+          const float ws = wsum[i];
+          const float inv = ws > 0.f ? 1.f / ws : 0.f;
+#pragma unroll
+          for (int q = 0; q < 8; q++) acc[q] *= inv;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const bf16 h0 = __float2bfloat16_rn(sv[q]), h1 = __float2bfloat16_rn(acc[q]);
+          sA[r * KP + q] = h0;
+          sAlo[r * KP + q] = __float2bfloat16_rn(sv[q] - __bfloat162float(h0));
+          sA[r * KP + DIN + q] = h1;
+          sAlo[r * KP + DIN + q] = __float2bfloat16_rn(acc[q] - __bfloat162float(h1));
+        }
+        if (AGf && i < Npad) {
+          reinterpret_cast<float4 *>(AGf + i * 8)[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+          reinterpret_cast<float4 *>(AGf + i * 8)[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
+        }
+      }
+    } else
     for (int r = threadIdx.x / LPR; r < MP_ROWS; r += RPP) {
       const int c8 = threadIdx.x % LPR;
       const ll i = base + r;
@@ -404,6 +457,19 @@ k_mp_fwd(const bf16 *__restrict__ Hin, const unsigned *__restrict__ ell,
         const bf16 *bp = sW + (nt * 8 + g) * KP + k0;
         mma_bf16(c[nt], a0, a1, a2, a3, *reinterpret_cast<const unsigned *>(bp),
                  *reinterpret_cast<const unsigned *>(bp + 8));
+      }
+      if (F32IN) {  // the low parts of the inputs, same weights
+        const bf16 *lr0 = sAlo + (warp * 16 + g) * KP, *lr1 = lr0 + 8 * KP;
+        const unsigned l0 = *reinterpret_cast<const unsigned *>(lr0 + k0);
+        const unsigned l1 = *reinterpret_cast<const unsigned *>(lr1 + k0);
+        const unsigned l2 = *reinterpret_cast<const unsigned *>(lr0 + k0 + 8);
+        const unsigned l3 = *reinterpret_cast<const unsigned *>(lr1 + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++) {
+          const bf16 *bp = sW + (nt * 8 + g) * KP + k0;
+          mma_bf16(c[nt], l0, l1, l2, l3, *reinterpret_cast<const unsigned *>(bp),
+                   *reinterpret_cast<const unsigned *>(bp + 8));
+        }
       }
     }
     const ll r0 = base + warp * 16 + g, r1 = r0 + 8;
@@ -532,17 +598,22 @@ k_mp_head_bwd(const float *__restrict__ dy, const bf16 *__restrict__ H3, ll Npad
 //   k_mp_gather_bwd (the graph is symmetric, so the scatter is a gather);
 //   dW += A^T dZ, db += sum of dZ rows (per block, FP32) -> partials.
 // INPUT_GRAD = false for the first layer (its inputs are the features).
-template <int DIN, bool INPUT_GRAD>
+// F32IN (first layer): Hprev (the features) and AG in FP32, split into high
+// and low BF16 parts for dW += A_hi^T dZ + A_lo^T dZ.
+template <int DIN, bool INPUT_GRAD, bool F32IN = false>
 __global__ void __launch_bounds__(MP_THREADS)
-k_mp_bwd(const bf16 *__restrict__ dZ, const bf16 *__restrict__ Hprev,
-         const bf16 *__restrict__ AG, const float *__restrict__ wsum, ll Npad,
+k_mp_bwd(const bf16 *__restrict__ dZ, const void *__restrict__ Hprev_,
+         const void *__restrict__ AG_, const float *__restrict__ wsum, ll Npad,
          const bf16 *__restrict__ Wb, float *__restrict__ dH, bf16 *__restrict__ U,
          float *__restrict__ part_w, float *__restrict__ part_b) {
   constexpr int K = 2 * DIN, KP = K + 8, ZP = MP_HID + 8;
   constexpr int NPAIR = (K / 16) * 8;              // (m-tile, n-tile) pairs of dW
   constexpr int PPW = NPAIR / (MP_THREADS / 32);  // per warp
+  const bf16 *__restrict__ Hprev = static_cast<const bf16 *>(Hprev_);
+  const bf16 *__restrict__ AG = static_cast<const bf16 *>(AG_);
   __shared__ __align__(16) bf16 sZ[MP_ROWS * ZP];
   __shared__ __align__(16) bf16 sA[MP_ROWS * KP];
+  __shared__ __align__(16) bf16 sAlo[F32IN ? MP_ROWS * KP : 8];
   __shared__ __align__(16) bf16 sW[INPUT_GRAD ? K * ZP : 8];
   if (INPUT_GRAD)
     for (int q = threadIdx.x; q < K * (MP_HID / 8); q += blockDim.x) {
@@ -565,11 +636,22 @@ k_mp_bwd(const bf16 *__restrict__ dZ, const bf16 *__restrict__ Hprev,
       *reinterpret_cast<uint4 *>(sZ + r * ZP + h8 * 8) =
           *reinterpret_cast<const uint4 *>(dZ + (base + r) * MP_HID + h8 * 8);
     }
-    for (int q = threadIdx.x; q < MP_ROWS * (K / 8); q += blockDim.x) {
-      const int r = q / (K / 8), k8 = q % (K / 8);
-      const bf16 *src = k8 < DIN / 8 ? Hprev + (base + r) * DIN + k8 * 8
-                                     : AG + (base + r) * DIN + (k8 - DIN / 8) * 8;
-      *reinterpret_cast<uint4 *>(sA + r * KP + k8 * 8) = *reinterpret_cast<const uint4 *>(src);
+    if (F32IN) {
+      const float *Hf = static_cast<const float *>(Hprev_), *Af = static_cast<const float *>(AG_);
+      for (int q = threadIdx.x; q < MP_ROWS * K; q += blockDim.x) {
+        const int r = q / K, k = q % K;
+        const float v = k < DIN ? Hf[(base + r) * DIN + k] : Af[(base + r) * DIN + k - DIN];
+        const bf16 h = __float2bfloat16_rn(v);
+        sA[r * KP + k] = h;
+        sAlo[r * KP + k] = __float2bfloat16_rn(v - __bfloat162float(h));
+      }
+    } else {
+      for (int q = threadIdx.x; q < MP_ROWS * (K / 8); q += blockDim.x) {
+        const int r = q / (K / 8), k8 = q % (K / 8);
+        const bf16 *src = k8 < DIN / 8 ? Hprev + (base + r) * DIN + k8 * 8
+                                       : AG + (base + r) * DIN + (k8 - DIN / 8) * 8;
+        *reinterpret_cast<uint4 *>(sA + r * KP + k8 * 8) = *reinterpret_cast<const uint4 *>(src);
+      }
     }
     __syncthreads();
     if (INPUT_GRAD) {
@@ -626,6 +708,12 @@ k_mp_bwd(const bf16 *__restrict__ dZ, const bf16 *__restrict__ Hprev,
         const unsigned b0 = pack_bf16(z0[0], z0[ZP]);
         const unsigned b1 = pack_bf16(z0[8 * ZP], z0[9 * ZP]);
         mma_bf16(cw[j], a0, a1, a2, a3, b0, b1);
+        if (F32IN) {
+          const bf16 *y0 = sAlo + rk * KP + mt * 16 + g;
+          mma_bf16(cw[j], pack_bf16(y0[0], y0[KP]), pack_bf16(y0[8], y0[KP + 8]),
+                   pack_bf16(y0[8 * KP], y0[9 * KP]), pack_bf16(y0[8 * KP + 8], y0[9 * KP + 8]),
+                   b0, b1);
+        }
       }
     }
     {
@@ -727,13 +815,32 @@ __global__ void k_mp_pred_to_elem(const int *__restrict__ perm, const float *__r
   if (i < N) out[perm[i]] = y[i];
 }
 
-__global__ void k_mp_feat_to_elem(const int *__restrict__ perm, const bf16 *__restrict__ X, ll N,
+__global__ void k_mp_feat_to_elem(const int *__restrict__ perm, const float *__restrict__ X, ll N,
                                   float *__restrict__ out) {
   const ll t = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N * MP_FIN) return;
   const ll i = t / MP_FIN;
   const int k = (int)(t % MP_FIN);
-  out[(ll)perm[i] * MP_FIN + k] = __bfloat162float(X[t]);
+  out[(ll)perm[i] * MP_FIN + k] = X[t];
+}
+
+// Geometric start: y = -sin(pi x~_1 / 2) along the group's principal axis,
+// the Fiedler vector of a uniform bar (a cosine over its length); FP64.
+__global__ void k_mp_geometric(const int *__restrict__ perm, const int *__restrict__ grp,
+                               const double *__restrict__ cent, ll nel,
+                               const double *__restrict__ frame, ll N, double *__restrict__ y) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int g = grp[i];
+  double v = 0.0;
+  if (g >= 0) {
+    const int e = perm[i];
+    const double *f = frame + (ll)g * 13;
+    const double x = cent[e] - f[0], yy = cent[nel + e] - f[1], z = cent[2 * nel + e] - f[2];
+    const double t = (f[3] * x + f[4] * yy + f[5] * z) * f[12];
+    v = -sin(1.5707963267948966 * t);
+  }
+  y[i] = v;
 }
 
 __global__ void k_mp_y_to_double(const float *__restrict__ y, const int *__restrict__ grp, ll N,
@@ -757,7 +864,8 @@ struct MpView {
 };
 
 struct MpBuffers {
-  DBuf<bf16> X, H[3], AG[3];
+  DBuf<float> X, AG0;  // first layer: FP32 features and neighbour means
+  DBuf<bf16> H[3], AG[3];
   DBuf<float> wsum, y;
   DBuf<float> dy, dH, part_w[3], part_b[3], part_head, grad;
   DBuf<bf16> dZa, dZb, U;
@@ -770,7 +878,22 @@ inline unsigned mp_grid(ll Npad) {
   return (unsigned)std::max<ll>(1, std::min<ll>(tiles, 152 * 8));
 }
 
+void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame);
+
 void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffers &B) {
+  cudaStream_t st = ctx().stream;
+  B.X.ensure((size_t)v.Npad * MP_FIN);
+  B.wsum.ensure((size_t)v.Npad);
+  DBuf<double> frame;
+  mp_frames(v, cent, nel, ndim, frame);
+  k_mp_features<<<grid_for(v.Npad, 256), 256, 0, st>>>(
+      v.perm, v.grp, cent, nel, frame.p, v.lv->ell.p, v.lv->slice_off.p, v.lv->slice_w.p, v.N,
+      v.Npad, B.X.p, B.wsum.p);
+  CK_LAUNCH();
+}
+
+// Per group: {mu[3], R[3][3], 1/s} (k_mp_frames).
+void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame) {
   cudaStream_t st = ctx().stream;
   const int G = (int)v.gstart.size();
   std::vector<FTile> tiles;
@@ -781,9 +904,7 @@ void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffer
       tiles.push_back({b, std::min(b + MP_FTILE, v.gstart[g] + v.gn[g]), g});
     nt[g] = (int)tiles.size() - t0[g];
   }
-  B.X.ensure((size_t)v.Npad * MP_FIN);
-  B.wsum.ensure((size_t)v.Npad);
-  DBuf<double> frame((size_t)std::max(G, 1) * 13);
+  frame.ensure((size_t)std::max(G, 1) * 13);
   if (G > 0 && !tiles.empty()) {
     DBuf<FTile> dt(tiles.size());
     DBuf<int> d0(G), dn(G);
@@ -800,10 +921,6 @@ void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffer
                                                   cent, nel, G, ndim, frame.p);
     CK_LAUNCH();
   }
-  k_mp_features<<<grid_for(v.Npad, 256), 256, 0, st>>>(
-      v.perm, v.grp, cent, nel, frame.p, v.lv->ell.p, v.lv->slice_off.p, v.lv->slice_w.p, v.N,
-      v.Npad, B.X.p, B.wsum.p);
-  CK_LAUNCH();
 }
 
 // keep: store every layer's activations and neighbour means for backward.
@@ -813,14 +930,14 @@ void mp_forward(const MpView &v, const NetDev &net, MpBuffers &B, bool keep) {
   B.H[0].ensure(nh), B.H[1].ensure(nh), B.y.ensure((size_t)v.Npad);
   if (keep) {
     B.H[2].ensure(nh);
-    B.AG[0].ensure((size_t)v.Npad * MP_FIN), B.AG[1].ensure(nh), B.AG[2].ensure(nh);
+    B.AG0.ensure((size_t)v.Npad * MP_FIN), B.AG[1].ensure(nh), B.AG[2].ensure(nh);
   }
   const Level &lv = *v.lv;
   const unsigned grid = mp_grid(v.Npad);
   const float *p = net.p;
-  k_mp_fwd<MP_FIN, false><<<grid, MP_THREADS, 0, st>>>(
+  k_mp_fwd<MP_FIN, false, true><<<grid, MP_THREADS, 0, st>>>(
       B.X.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, B.wsum.p, v.N, v.Npad, net.Wf[0],
-      p + MP_OFF_B1, B.H[0].p, keep ? B.AG[0].p : nullptr, nullptr, nullptr, nullptr);
+      p + MP_OFF_B1, B.H[0].p, keep ? B.AG0.p : nullptr, nullptr, nullptr, nullptr);
   CK_LAUNCH();
   k_mp_fwd<MP_HID, false><<<grid, MP_THREADS, 0, st>>>(
       B.H[0].p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, B.wsum.p, v.N, v.Npad, net.Wf[1],
@@ -875,9 +992,9 @@ double mp_backward(const MpView &v, const NetDev &net, MpBuffers &B) {
   k_mp_gather_bwd<<<gg, MP_THREADS, 0, st>>>(B.dH.p, B.U.p, B.H[0].p, lv.ell.p, lv.slice_off.p,
                                              lv.slice_w.p, v.N, v.Npad, B.dZa.p);
   CK_LAUNCH();
-  k_mp_bwd<MP_FIN, false><<<MP_GB, MP_THREADS, 0, st>>>(B.dZa.p, B.X.p, B.AG[0].p, B.wsum.p,
-                                                        v.Npad, nullptr, nullptr, nullptr,
-                                                        B.part_w[0].p, B.part_b[0].p);
+  k_mp_bwd<MP_FIN, false, true><<<MP_GB, MP_THREADS, 0, st>>>(
+      B.dZa.p, B.X.p, B.AG0.p, B.wsum.p, v.Npad, nullptr, nullptr, nullptr, B.part_w[0].p,
+      B.part_b[0].p);
   CK_LAUNCH();
   k_mp_grad_reduce<<<grid_for(MP_NPARAM, 256), 256, 0, st>>>(
       B.part_w[0].p, B.part_b[0].p, B.part_w[1].p, B.part_b[1].p, B.part_w[2].p, B.part_b[2].p,
@@ -921,6 +1038,18 @@ bool warm_net_ready() {
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return false;
   std::lock_guard<std::mutex> lk(g_net_mu);
   return g_net[dev].ready;
+}
+
+void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
+                             const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
+                             const std::vector<ll> &gn, ll N, double *y) {
+  MpView v;
+  v.lv = &lv, v.perm = perm, v.grp = grp, v.N = N, v.Npad = (N + MP_ROWS - 1) / MP_ROWS * MP_ROWS;
+  v.gstart = gstart, v.gn = gn;
+  DBuf<double> frame;
+  mp_frames(v, cent, nel, ndim, frame);
+  k_mp_geometric<<<grid_for(N, 256), 256, 0, ctx().stream>>>(perm, grp, cent, nel, frame.p, N, y);
+  CK_LAUNCH();
 }
 
 void warm_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,

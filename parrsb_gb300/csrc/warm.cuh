@@ -42,4 +42,10 @@ void warm_predict_level(const Level &lv, const int *perm, const int *grp, const 
                         ll nel, int ndim, const std::vector<ll> &gstart,
                         const std::vector<ll> &gn, ll N, double *y);
 
+// The geometric start of the same groups: -sin(pi x~_1 / 2) along each
+// group's principal axis (x~_1 as in the network's first input feature).
+void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
+                             const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
+                             const std::vector<ll> &gn, ll N, double *y);
+
 }  // namespace prsb

@@ -6,8 +6,8 @@ this module drives them through the C ABI:
 
 * ``training_meshes(count, seed)`` -- the seeded training set: jittered hex
   sub-boxes (distinct side lengths, so every box has a well separated
-  Fiedler vector) and annular hex cylinders longer than wide, 1k-64k
-  elements each, log-uniform;
+  Fiedler vector) and annular hex cylinders with more elements along the
+  axis than around it, 1k-64k elements each, log-uniform;
 * ``label(vtx, group, ngroups)`` -- their Fiedler vectors by the plain
   method (parrsb_fiedler_groups: batched Lanczos, FP64 vectors);
 * ``train(...)`` -- Adam on the sign-invariant cosine loss, every step a
@@ -96,15 +96,15 @@ def training_meshes(count=2000, seed=0, smin=1000, smax=64000):
                                    seed=seed * 7919 + m, hi=tuple(hi), id_offset=off)
             off += int(np.prod(dims + 1))
         else:
-            # annular cylinder, r in [1, 2], longer than wide
-            nr = int(rng.integers(2, 7))
-            nt = max(8, int(round(2 * np.pi * 1.5 / (1.0 / nr))))
-            nz = max(4, int(round(target / (nt * nr))))
-            length = nz * (1.0 / nr)
-            if length < 6.0:
-                length = 6.0
+            # annular cylinder, r in [1, 2], near-cubic elements, more
+            # elements along the axis than around it (the graph Laplacian
+            # sees element counts, not lengths: its Fiedler vector then runs
+            # along the axis, like the centroids' principal axis)
+            nr = max(2, min(8, int((target / 75.0) ** (1.0 / 3.0))))
+            nt = max(8, int(round(2 * np.pi * 1.5 * nr)))
+            nz = max(int(np.ceil(0.8 * nt)), int(round(target / (nt * nr))))
             v, x = meshgen.pipe_hex(nt, nr, nz, jitter=0.05, seed=seed * 7919 + m,
-                                    length=length)
+                                    length=nz / nr)
             v = v + off
             off += nt * (nr + 1) * (nz + 1)
         vts.append(v)
@@ -115,9 +115,22 @@ def training_meshes(count=2000, seed=0, smin=1000, smax=64000):
 
 
 def label(vtx, group, ngroups, **kw):
-    """Fiedler vectors of every group by the plain method (FP64 vectors)."""
+    """Fiedler vectors of every group by the plain method (FP64 vectors,
+    batched Lanczos from the reference's start), restarted until each
+    vector's eigen-residual is at most rsb_tol (default 1e-6)."""
     kw.setdefault("rsb_tol", 1e-6)
-    f, it, rs = fiedler_groups(vtx, group, ngroups, batched=True, **kw)
+    kw.setdefault("rsb_max_passes", 400)
+    old = {k: os.environ.get(k) for k in ("PARRSB_GPU_RESID_STOP", "PARRSB_GPU_FP32")}
+    os.environ["PARRSB_GPU_RESID_STOP"] = "1"
+    os.environ["PARRSB_GPU_FP32"] = "0"
+    try:
+        f, it, rs = fiedler_groups(vtx, group, ngroups, batched=True, **kw)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     return f, it, rs
 
 
@@ -183,7 +196,7 @@ def adam(d_params, d_m, d_v, d_grad, step, lr):
         raise ParrsbError(rc, "parrsb_warm_adam")
 
 
-def train(count=2000, seed=0, epochs=30, nbatch=8, lr=2e-3, params=None, log=None):
+def train(count=2000, seed=0, epochs=200, nbatch=8, lr=3e-3, params=None, log=None):
     """Train on `count` seeded meshes split into `nbatch` batches; returns
     (params, history).  history: per epoch mean training loss, and the
     loss of the held-out last batch."""
@@ -226,6 +239,7 @@ def train(count=2000, seed=0, epochs=30, nbatch=8, lr=2e-3, params=None, log=Non
             log(hist[-1])
     info = {"label_s": t_label, "train_s": time.time() - t1, "elements": int(len(vtx)),
             "label_steps_mean": float(np.mean(it)), "label_resid_max": float(np.max(rs)),
+            "label_resid_p90": float(np.percentile(rs, 90)),
             "history": hist}
     for b, _ in batches:
         b.close()
@@ -238,8 +252,8 @@ if __name__ == "__main__":
     import torch
     ap = argparse.ArgumentParser(description="train the warm-start network on the GPU")
     ap.add_argument("--count", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=30)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--log", default=None)
