@@ -469,7 +469,9 @@ def main():
         starts = {}
         legs = [("reference_start", {}), ("random_start", {"PARRSB_GPU_START": "1"}),
                 ("geometric_start", {"PARRSB_GPU_START": "2"}),
-                ("reference_start_resid_stop", {"PARRSB_GPU_RESID_STOP": "1"})]
+                ("reference_start_resid_stop", {"PARRSB_GPU_RESID_STOP": "1"}),
+                ("geometric_start_resid_stop", {"PARRSB_GPU_START": "2",
+                                                "PARRSB_GPU_RESID_STOP": "1"})]
         if warm_ok:
             legs += [("warm_start", {"PARRSB_GPU_WARM": "1"}),
                      ("warm_start_resid_stop", {"PARRSB_GPU_WARM": "1",

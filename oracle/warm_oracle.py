@@ -86,11 +86,13 @@ def frames(cent, group):
 
 
 def features(cent, group, rows, w):
-    """Input features per element: x~ (3), weighted degree / 56, zeros."""
+    """Input features per element: x~ (3), weighted degree / 56, the
+    geometric guess -sin(pi x~_1 / 2), zeros."""
     X = np.zeros((len(cent), FIN))
     for g, (mu, R, inv_s) in frames(cent, group).items():
         sel = group == g
         X[sel, :3] = ((cent[sel] - mu) @ R.T) * inv_s
+        X[sel, 4] = -np.sin(np.pi * X[sel, 0] / 2)
     deg = np.bincount(rows, weights=w, minlength=len(cent))
     X[:, 3] = np.where(group >= 0, deg * DEG_SCALE, 0.0)
     return X
@@ -116,7 +118,7 @@ def forward(X, rows, col, w, params, round_weights=True):
         cache.setdefault("A", []).append(A)
         cache.setdefault("Z", []).append(Z)
         cache["H"].append(H)
-    y = H @ P["wo"] + P["bo"]
+    y = H @ P["wo"] + P["bo"] + X[:, 4]  # the head corrects the geometric guess
     return y, cache
 
 

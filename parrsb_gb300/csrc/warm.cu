@@ -15,7 +15,9 @@
 //   h_l = relu([h_{l-1} | a_l] W_l + b_l),  a_l,i = sum_j w_ij h_{l-1},j /
 //                                                    sum_j w_ij
 // (BF16 activations and weights, FP32 accumulation on the tensor cores with
-// mma.sync m16n8k16), then y = h_3 . wo + bo.  The training step (forward,
+// mma.sync m16n8k16), then y = g + h_3 . wo + bo: the head corrects the
+// geometric guess g = -sin(pi x~_1 / 2), which is also an input.  The
+// training step (forward,
 // sign-invariant cosine loss against the Fiedler vectors of the plain
 // method, backward, Adam) runs on the same kernels; its C entry points are
 // at the end of this file.
@@ -266,8 +268,8 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
   f[12] = inv_s;
 }
 
-// Input features of every position: X[i] = (x~ (3), deg / 56, 0, 0, 0, 0)
-// in FP32 (the first layer multiplies them as a pair of BF16 values, high
+// Input features of every position: X[i] = (x~ (3), deg / 56, g, 0, 0, 0)
+// with g = -sin(pi x~_1 / 2), in FP32 (the first layer multiplies them as a pair of BF16 values, high
 // and low part, so positions keep about 16 significant bits: a group may
 // be thousands of elements long); rows outside the groups (grp < 0) and
 // padding rows are zero.
@@ -295,6 +297,10 @@ __global__ void k_mp_features(const int *__restrict__ perm, const int *__restric
     for (int k = 0; k < wd; k++) acc += ep[(ll)k * 32] >> 28;
     ws = (float)acc;
     v[3] = (float)((double)acc * MP_DEG_SCALE);
+    // the geometric guess -sin(pi x~_1 / 2) (the Fiedler vector of a uniform
+    // bar along the first axis): an input, and the start the head corrects
+    const double t = (f[3] * x + f[4] * y + f[5] * z) * f[12];
+    v[4] = (float)(-sin(1.5707963267948966 * t));
   }
   float4 *o = reinterpret_cast<float4 *>(X + i * MP_FIN);
   o[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -355,7 +361,8 @@ k_mp_fwd(const void *__restrict__ Hin_, const unsigned *__restrict__ ell,
          const ll *__restrict__ slice_off, const int *__restrict__ slice_w,
          const float *__restrict__ wsum, ll N, ll Npad, const bf16 *__restrict__ Wf,
          const float *__restrict__ bias, bf16 *__restrict__ Hout, void *__restrict__ AG_,
-         const float *__restrict__ wo, const float *__restrict__ bo, float *__restrict__ y) {
+         const float *__restrict__ wo, const float *__restrict__ bo, float *__restrict__ y,
+         const float *__restrict__ Xg) {
   constexpr int K = 2 * DIN, KP = K + 8;
   const bf16 *__restrict__ Hin = static_cast<const bf16 *>(Hin_);
   bf16 *__restrict__ AG = static_cast<bf16 *>(AG_);
@@ -498,9 +505,9 @@ k_mp_fwd(const void *__restrict__ Hin_, const unsigned *__restrict__ ell,
       y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
       y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
       y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
-      if (tig == 0) {
-        y[r0] = y0 + bo[0];
-        y[r1] = y1 + bo[0];
+      if (tig == 0) {  // the head corrects the geometric guess (feature 4)
+        y[r0] = y0 + bo[0] + Xg[r0 * MP_FIN + 4];
+        y[r1] = y1 + bo[0] + Xg[r1 * MP_FIN + 4];
       }
     }
   }
@@ -937,16 +944,16 @@ void mp_forward(const MpView &v, const NetDev &net, MpBuffers &B, bool keep) {
   const float *p = net.p;
   k_mp_fwd<MP_FIN, false, true><<<grid, MP_THREADS, 0, st>>>(
       B.X.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, B.wsum.p, v.N, v.Npad, net.Wf[0],
-      p + MP_OFF_B1, B.H[0].p, keep ? B.AG0.p : nullptr, nullptr, nullptr, nullptr);
+      p + MP_OFF_B1, B.H[0].p, keep ? B.AG0.p : nullptr, nullptr, nullptr, nullptr, nullptr);
   CK_LAUNCH();
   k_mp_fwd<MP_HID, false><<<grid, MP_THREADS, 0, st>>>(
       B.H[0].p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, B.wsum.p, v.N, v.Npad, net.Wf[1],
-      p + MP_OFF_B2, B.H[1].p, keep ? B.AG[1].p : nullptr, nullptr, nullptr, nullptr);
+      p + MP_OFF_B2, B.H[1].p, keep ? B.AG[1].p : nullptr, nullptr, nullptr, nullptr, nullptr);
   CK_LAUNCH();
   k_mp_fwd<MP_HID, true><<<grid, MP_THREADS, 0, st>>>(
       B.H[1].p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, B.wsum.p, v.N, v.Npad, net.Wf[2],
       p + MP_OFF_B3, keep ? B.H[2].p : nullptr, keep ? B.AG[2].p : nullptr, p + MP_OFF_WO,
-      p + MP_OFF_BO, B.y.p);
+      p + MP_OFF_BO, B.y.p, B.X.p);
   CK_LAUNCH();
 }
 

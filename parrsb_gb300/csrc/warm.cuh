@@ -11,9 +11,10 @@ namespace prsb {
 
 // Network shape.  Per element: 8 input features (the element centroid in
 // its group's principal frame, scaled so the longest axis spans about
-// [-1, 1]; the element's weighted degree / 56; four zeros), three layers
+// [-1, 1]; the element's weighted degree / 56; the geometric guess
+// g = -sin(pi x~_1 / 2); three zeros), three layers
 //   h_l = relu([h_{l-1} | mean_w(h_{l-1} over the graph neighbours)] W_l + b_l)
-// of width 64, and a linear head y = h_3 . wo + bo.
+// of width 64, and a head that corrects the guess: y = g + h_3 . wo + bo.
 constexpr int MP_HID = 64;
 constexpr int MP_FIN = 8;
 constexpr int MP_K1 = 2 * MP_FIN;   // 16

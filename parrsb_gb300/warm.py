@@ -40,7 +40,8 @@ def init_params(seed=0):
     for k in (K1, K2, K2):
         parts.append(rng.normal(0.0, np.sqrt(2.0 / k), k * HID))
         parts.append(np.zeros(HID))
-    parts.append(rng.normal(0.0, np.sqrt(1.0 / HID), HID))
+    # small head: the network starts at the geometric guess it corrects
+    parts.append(rng.normal(0.0, 1e-3, HID))
     parts.append(np.zeros(1))
     p = np.concatenate(parts).astype(np.float32)
     assert p.size == NPARAM

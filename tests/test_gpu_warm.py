@@ -55,8 +55,8 @@ def test_features_match_restatement():
     rows, col, w = _graph(vtx, group)
     Xo = W.features(O.centroids(xyz, 8), group.astype(np.int64), rows, w)
     # FP32 features computed in FP64 (Jacobi frames on the GPU, LAPACK here)
-    np.testing.assert_allclose(X[:, :4], Xo[:, :4], rtol=1e-5, atol=1e-6)
-    assert np.all(X[:, 4:] == 0)
+    np.testing.assert_allclose(X[:, :5], Xo[:, :5], rtol=1e-5, atol=1e-6)
+    assert np.all(X[:, 5:] == 0)
 
 
 def _gpu_step(b, params, label):
@@ -78,6 +78,7 @@ def test_forward_and_gradient_match_fp64_restatement():
     rng = np.random.default_rng(7)
     params = Wm.init_params(11).astype(np.float64)
     params[W.OFF["b1"][0]:W.OFF["b1"][1]] = rng.normal(0, 0.1, 64)
+    params[W.OFF["wo"][0]:W.OFF["wo"][1]] = rng.normal(0, 0.1, 64)  # a head that matters
     label = np.ascontiguousarray(np.cos(np.pi * X[:, 0] * 0.5) + 0.1 * rng.normal(size=len(X)))
     loss, pred, grad = _gpu_step(b, params, label)
     b.close()

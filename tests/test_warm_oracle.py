@@ -41,7 +41,8 @@ def test_features_axis_aligned_box():
     assert np.allclose(np.abs(X[:, 0]).max(), 11 / 12 * np.sqrt(12 ** 2 / (12 ** 2 - 1)), rtol=1e-9)
     assert np.all(np.diff(X[:12, 0]) > 0)  # x increases along the first row
     assert np.isclose(X[:, 3].max(), 1.0)
-    assert np.all(X[:, 4:] == 0)
+    np.testing.assert_allclose(X[:, 4], -np.sin(np.pi * X[:, 0] / 2))
+    assert np.all(X[:, 5:] == 0)
 
 
 def test_gradient_matches_finite_differences():
