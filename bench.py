@@ -467,15 +467,17 @@ def main():
     starts = None
     if not args.no_plain:
         starts = {}
+        RS = {"PARRSB_GPU_RESID_STOP": "1"}
         legs = [("reference_start", {}), ("random_start", {"PARRSB_GPU_START": "1"}),
                 ("geometric_start", {"PARRSB_GPU_START": "2"}),
-                ("reference_start_resid_stop", {"PARRSB_GPU_RESID_STOP": "1"}),
-                ("geometric_start_resid_stop", {"PARRSB_GPU_START": "2",
-                                                "PARRSB_GPU_RESID_STOP": "1"})]
+                ("reference_start_resid_stop", dict(RS)),
+                ("geometric_start_resid_stop", dict(RS, PARRSB_GPU_START="2"))]
         if warm_ok:
-            legs += [("warm_start", {"PARRSB_GPU_WARM": "1"}),
-                     ("warm_start_resid_stop", {"PARRSB_GPU_WARM": "1",
-                                                "PARRSB_GPU_RESID_STOP": "1"})]
+            legs += [("learned_start", {"PARRSB_GPU_WARM": "1"}),
+                     ("learned_start_resid_stop", dict(RS, PARRSB_GPU_WARM="1")),
+                     ("learned_1M_geometric_resid_stop",
+                      dict(RS, PARRSB_GPU_WARM="1", PARRSB_GPU_START="2",
+                           PARRSB_GPU_WARM_MIN="1048576"))]
         for name, env in legs:
             saved = {k: os.environ.get(k) for k in env}
             os.environ.update(env)

@@ -1586,12 +1586,14 @@ struct Lanczos {
   // first pass removes its mean and normalises it.
   void random_vector() { tile<TM_RANDOM, GATE_ALL>(); }
 
-  // Start vectors with a learned candidate y (FP64 per position): every
-  // group starts from y or from the fallback start (start_kind 0: the
-  // reference's step vector, 1: random), whichever has the lower FP64
-  // eigen-residual ||L f - rho f|| / ||f|| (the judge).  Groups smaller
-  // than warm_min keep the fallback.  Leaves the start in f.
-  void choose_start(const Level &lv, const double *y, int start_kind, ll warm_min) {
+  // Start vectors with a predicted candidate y (FP64 per position): every
+  // group starts from y or from the fallback start (start_kind 1: random,
+  // otherwise the reference's step vector), whichever has the lower FP64
+  // eigen-residual ||L f - rho f|| / ||f|| (the judge); groups flagged in
+  // degen (two nearly equal principal axes) keep the fallback.  Leaves the
+  // start in f.
+  void choose_start(const Level &lv, const double *y, int start_kind,
+                    const std::vector<int> &degen) {
     cudaStream_t st = ctx().stream;
     k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
     CK_LAUNCH();
@@ -1612,12 +1614,13 @@ struct Lanczos {
     long long tried = 0;
     std::vector<int> use(A, 0);
     for (int g = 0; g < A; g++) {
-      if (hgs[g].n < warm_min) continue;
       const double rw = hgs[g].resid;
       tried++;
       lf += log10(std::max(r_fb[g], 1e-300));
       lw += log10(std::max(rw, 1e-300));
-      use[g] = rw < r_fb[g] ? 1 : 0;  // NaN never wins
+      // a group with two axes of nearly the same length keeps the fallback
+      const bool dg = g < (int)degen.size() && degen[g];
+      use[g] = (!dg && rw < r_fb[g]) ? 1 : 0;  // NaN never wins
       S.warm_used += use[g];
     }
     // running geometric means over every judged group of the call
@@ -2264,12 +2267,12 @@ template <typename VT>
 void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
                        const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N,
                        double *f_pos, std::vector<GState> &res,
-                       const double *y_warm = nullptr) {
+                       const double *y_warm = nullptr, const std::vector<int> &degen = {}) {
   lz.setup(gstart, gn, N, o.miter);
   lz.resid_stop = o.resid_stop != 0;
   {
     StageTimer tm(PARRSB_STAGE_LANCZOS);
-    if (y_warm) lz.choose_start(lv, y_warm, o.start, o.warm_min);
+    if (y_warm) lz.choose_start(lv, y_warm, o.start, degen);
     lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, y_warm != nullptr, o.start);
   }
   if (o.check_resid) lz.residual(lv);
@@ -2432,22 +2435,27 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     }
     // ---- learned warm start: predictions for the groups of this level
     // that are large enough (the judge in Lanczos::choose_start decides)
+    // (the network where groups have at least warm_min elements; with
+    // start 2 the geometric guess elsewhere)
     const double *y_warm = nullptr;
+    std::vector<int> degen;
     if ((o.warm || o.start == 2) && nv == 8) {
       ll biggest = 0;
       for (int g = 0; g < na; g++) biggest = std::max(biggest, an[g]);
-      if (biggest >= std::max<ll>(o.warm_min, 2)) {
-        if (o.warm && !warm_net_ready())
+      const bool use_net = o.warm && biggest >= std::max<ll>(o.warm_min, 2);
+      if (use_net || o.start == 2) {
+        if (use_net && !warm_net_ready())
           throw ArgError{PARRSB_ERR_ARGS, "warm start requested but no network installed"};
         cudaEvent_t w0, w1;
         CK(cudaEventCreate(&w0));
         CK(cudaEventCreate(&w1));
         CK(cudaEventRecord(w0, st));
         y_pred.ensure((size_t)N);
-        if (o.warm)
-          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
-        else  // start 2: the geometric start in place of the network
-          geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p);
+        if (use_net)
+          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p, &degen);
+        else  // start 2: the geometric guess
+          geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p,
+                                  &degen);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;
@@ -2461,7 +2469,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     // ---- Fiedler vectors (src/rsb.c:300-302)
     std::vector<GState> res;
     if (o.batched) {
-      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res, y_warm);
+      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res, y_warm, degen);
     } else {
       // plain path: every group of the level solved by its own launches
       RsbOpts o1 = o;
@@ -2469,7 +2477,8 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
       for (int g = 0; g < na; g++) {
         std::vector<GState> r1;
         std::vector<ll> s1 = {ast[g]}, n1 = {an[g]};
-        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1, y_warm);
+        std::vector<int> d1 = {g < (int)degen.size() ? degen[g] : 0};
+        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1, y_warm, d1);
         CK(cudaMemcpyAsync(f_pos.p + ast[g], f_tmp.p + ast[g], an[g] * sizeof(double),
                            cudaMemcpyDeviceToDevice, st));
         res.push_back(r1[0]);

@@ -203,7 +203,8 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
                             const int *__restrict__ tile0, const int *__restrict__ ntile,
                             const ll *__restrict__ gstart, const ll *__restrict__ gn,
                             const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
-                            int ngroups, int ndim, double *__restrict__ frame) {
+                            int ngroups, int ndim, double *__restrict__ frame,
+                            int *__restrict__ degen) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngroups) return;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -237,6 +238,7 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) R[a][k] = V[k][ord[a]];
   const double l1 = d[ord[0]], l2 = d[ord[1]];
+  degen[g] = (l1 > 0.0 && (l1 - l2) <= 0.05 * l1) ? 1 : 0;
   if (l1 > 0.0 && (l1 - l2) <= 0.05 * l1) {
     int ax = 0;  // coordinate axis of largest variance (first strict maximum)
     for (int k = 1; k < 3; k++)
@@ -885,22 +887,26 @@ inline unsigned mp_grid(ll Npad) {
   return (unsigned)std::max<ll>(1, std::min<ll>(tiles, 152 * 8));
 }
 
-void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame);
+void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame,
+               std::vector<int> *degen = nullptr);
 
-void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffers &B) {
+void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffers &B,
+                 std::vector<int> *degen = nullptr) {
   cudaStream_t st = ctx().stream;
   B.X.ensure((size_t)v.Npad * MP_FIN);
   B.wsum.ensure((size_t)v.Npad);
   DBuf<double> frame;
-  mp_frames(v, cent, nel, ndim, frame);
+  mp_frames(v, cent, nel, ndim, frame, degen);
   k_mp_features<<<grid_for(v.Npad, 256), 256, 0, st>>>(
       v.perm, v.grp, cent, nel, frame.p, v.lv->ell.p, v.lv->slice_off.p, v.lv->slice_w.p, v.N,
       v.Npad, B.X.p, B.wsum.p);
   CK_LAUNCH();
 }
 
-// Per group: {mu[3], R[3][3], 1/s} (k_mp_frames).
-void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame) {
+// Per group: {mu[3], R[3][3], 1/s} (k_mp_frames); degen (optional): per
+// group, 1 when its two largest centroid variances are within 5%.
+void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame,
+               std::vector<int> *degen) {
   cudaStream_t st = ctx().stream;
   const int G = (int)v.gstart.size();
   std::vector<FTile> tiles;
@@ -912,6 +918,7 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     nt[g] = (int)tiles.size() - t0[g];
   }
   frame.ensure((size_t)std::max(G, 1) * 13);
+  DBuf<int> dg((size_t)std::max(G, 1));
   if (G > 0 && !tiles.empty()) {
     DBuf<FTile> dt(tiles.size());
     DBuf<int> d0(G), dn(G);
@@ -925,8 +932,13 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     k_mp_moments<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, gs.p, v.perm, cent, nel, part.p);
     CK_LAUNCH();
     k_mp_frames<<<grid_for(G, 128), 128, 0, st>>>(dt.p, part.p, d0.p, dn.p, gs.p, gn.p, v.perm,
-                                                  cent, nel, G, ndim, frame.p);
+                                                  cent, nel, G, ndim, frame.p, dg.p);
     CK_LAUNCH();
+  }
+  if (degen) {
+    degen->assign(G, 0);
+    d2h(degen->data(), dg.p, (size_t)G);
+    sync();
   }
 }
 
@@ -1049,19 +1061,20 @@ bool warm_net_ready() {
 
 void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
                              const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
-                             const std::vector<ll> &gn, ll N, double *y) {
+                             const std::vector<ll> &gn, ll N, double *y,
+                             std::vector<int> *degen) {
   MpView v;
   v.lv = &lv, v.perm = perm, v.grp = grp, v.N = N, v.Npad = (N + MP_ROWS - 1) / MP_ROWS * MP_ROWS;
   v.gstart = gstart, v.gn = gn;
   DBuf<double> frame;
-  mp_frames(v, cent, nel, ndim, frame);
+  mp_frames(v, cent, nel, ndim, frame, degen);
   k_mp_geometric<<<grid_for(N, 256), 256, 0, ctx().stream>>>(perm, grp, cent, nel, frame.p, N, y);
   CK_LAUNCH();
 }
 
 void warm_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
                         ll nel, int ndim, const std::vector<ll> &gstart,
-                        const std::vector<ll> &gn, ll N, double *y) {
+                        const std::vector<ll> &gn, ll N, double *y, std::vector<int> *degen) {
   int dev = 0;
   CK(cudaGetDevice(&dev));
   NetDev net;
@@ -1076,7 +1089,7 @@ void warm_predict_level(const Level &lv, const int *perm, const int *grp, const 
   v.lv = &lv, v.perm = perm, v.grp = grp, v.N = N, v.Npad = (N + MP_ROWS - 1) / MP_ROWS * MP_ROWS;
   v.gstart = gstart, v.gn = gn;
   MpBuffers B;
-  mp_features(v, cent, nel, ndim, B);
+  mp_features(v, cent, nel, ndim, B, degen);
   mp_forward(v, net, B, false);
   k_mp_y_to_double<<<grid_for(N, 256), 256, 0, ctx().stream>>>(B.y.p, grp, N, y);
   CK_LAUNCH();
