@@ -37,6 +37,9 @@ def _compile(src, extra):
     cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", path, "-o", obj + ".tmp"]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
+        # a failed compile is an error even when an older object exists
+        if os.path.exists(obj):
+            os.remove(obj)
         return obj, p.stdout + p.stderr
     os.replace(obj + ".tmp", obj)
     return obj, (p.stdout + p.stderr) if ("warning" in p.stderr.lower()) else None

@@ -38,15 +38,22 @@ bool warm_net_ready();
 // Predicted Fiedler vectors of the groups [gstart[g], gstart[g] + gn[g]) of
 // a level (perm: element at each position; grp: group of each position, -1
 // for none; cent: centroids [3][nel] in element order): y[i] for every
-// position i (0 outside the groups), FP64, on the library stream.
+// position i (0 outside the groups), FP64, on the library stream.  degen
+// (optional, host): per group, 1 when the two largest variances of its
+// centroids are within 5% (two axes of nearly the same length: the leading
+// eigenvalues of the group's Laplacian are nearly equal, and no prediction
+// can say which combination Lanczos will settle on; the reference's step
+// start keeps the split of the pre-partition).
 void warm_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
                         ll nel, int ndim, const std::vector<ll> &gstart,
-                        const std::vector<ll> &gn, ll N, double *y);
+                        const std::vector<ll> &gn, ll N, double *y,
+                        std::vector<int> *degen = nullptr);
 
 // The geometric start of the same groups: -sin(pi x~_1 / 2) along each
 // group's principal axis (x~_1 as in the network's first input feature).
 void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
                              const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
-                             const std::vector<ll> &gn, ll N, double *y);
+                             const std::vector<ll> &gn, ll N, double *y,
+                             std::vector<int> *degen = nullptr);
 
 }  // namespace prsb
