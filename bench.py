@@ -422,7 +422,21 @@ def main():
     # ---- end to end (host buffers, copies inside the timed region)
     t_e2e = None
     e2e_stages = None
+    link = None
     if not args.no_e2e:
+        # this machine's host-to-device bandwidth from the same pinned buffers
+        # into the device copies (the e2e leg's extra time is mostly this)
+        lt = []
+        for _ in range(4):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d_vtx.copy_(h_vtx, non_blocking=True)
+            d_xyz.copy_(h_xyz, non_blocking=True)
+            torch.cuda.synchronize()
+            lt.append(time.perf_counter() - t0)
+        t_link = statistics.median(lt[1:])
+        link = {"h2d_gbs": (vtx.nbytes + xyz.nbytes) / t_link / 1e9,
+                "h2d_ms_for_inputs": round(t_link * 1e3, 2)}
         step_host()
         barrier()
         t0 = time.perf_counter()
@@ -569,7 +583,8 @@ def main():
         "method": {"batched": "all groups of a level per launch, one CUDA graph per pass",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(part.nbytes), "last_call": e2e_stages},
+                "d2h_bytes_per_step": int(part.nbytes), "last_call": e2e_stages,
+                "link": link},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": tr_val, "kernel": "k_spmv (sliced-ELL Laplacian)",

@@ -57,13 +57,29 @@ def restrict(rowptr, col, w, group):
     return rows[keep], np.asarray(col)[keep], np.asarray(w, np.float64)[keep]
 
 
-def frames(cent, group):
+def spacings(cent, group, rows, cols, w, wface=4):
+    """Per group and axis: 1 / h_a with h_a^2 the mean of (c_i,a - c_j,a)^2
+    over the face neighbour pairs (weight wface) inside the group."""
+    out = {}
+    face = w == wface
+    for g in np.unique(group[group >= 0]):
+        sel = face & (group[rows] == g)
+        d = cent[rows[sel]] - cent[cols[sel]]
+        cnt = sel.sum()
+        h2 = (d * d).sum(axis=0) / cnt if cnt else np.zeros(3)
+        out[int(g)] = np.where(h2 > 0, 1.0 / np.sqrt(np.where(h2 > 0, h2, 1.0)), 1.0)
+    return out
+
+
+def frames(cent, group, rows, cols, w):
     """Per group: mean, principal axes (rows, largest variance first, largest
     component positive; axes within 5% take the first inside their plane
-    along the coordinate axis of largest variance) and 1 / sqrt(3 l1 / n)."""
+    along the coordinate axis of largest variance) and 1 / sqrt(3 l1 / n),
+    all of the centroids measured in element spacings (spacings())."""
     out = {}
+    sp = spacings(cent, group, rows, cols, w)
     for g in np.unique(group[group >= 0]):
-        c = cent[group == g]
+        c = cent[group == g] * sp[int(g)]
         n = len(c)
         mu = c.mean(axis=0)
         d = c - mu
@@ -81,17 +97,17 @@ def frames(cent, group):
             if R[a, np.argmax(np.abs(R[a]))] < 0:
                 R[a] = -R[a]
         inv_s = 1.0 / np.sqrt(3.0 * lam[0] / n) if lam[0] > 0 else 0.0
-        out[int(g)] = (mu, R, inv_s)
+        out[int(g)] = (mu, R, inv_s, sp[int(g)])
     return out
 
 
-def features(cent, group, rows, w):
+def features(cent, group, rows, cols, w):
     """Input features per element: x~ (3), weighted degree / 56, the
     geometric guess -sin(pi x~_1 / 2), zeros."""
     X = np.zeros((len(cent), FIN))
-    for g, (mu, R, inv_s) in frames(cent, group).items():
+    for g, (mu, R, inv_s, k) in frames(cent, group, rows, cols, w).items():
         sel = group == g
-        X[sel, :3] = ((cent[sel] - mu) @ R.T) * inv_s
+        X[sel, :3] = ((cent[sel] * k - mu) @ R.T) * inv_s
         X[sel, 4] = -np.sin(np.pi * X[sel, 0] / 2)
     deg = np.bincount(rows, weights=w, minlength=len(cent))
     X[:, 3] = np.where(group >= 0, deg * DEG_SCALE, 0.0)

@@ -36,6 +36,7 @@ namespace {
 constexpr int MP_ROWS = 64;        // rows per tile of the layer kernels (4 warps x 16)
 constexpr int MP_THREADS = 128;
 constexpr int MP_FTILE = 16384;    // rows per tile of the group-frame reductions
+constexpr int MP_FRAME = 16;       // doubles per group frame
 constexpr double MP_DEG_SCALE = 1.0 / 56.0;  // hex: 6 x 4 + 12 x 2 + 8 x 1
 
 // Block-wide sum in a fixed order (shuffle tree per warp, then the warps in
@@ -130,19 +131,74 @@ struct FTile {
   int g;
 };
 
+// Element spacing per axis.  The graph Laplacian sees element counts, not
+// lengths: a box of 256 x 256 x 128 elements on the unit cube has its
+// Fiedler vector along x or y although z is as long.  So centroids are
+// measured in element spacings: per group and axis a, h_a^2 = mean over the
+// face neighbour pairs (weight wface) of (c_i,a - c_j,a)^2, and the frame
+// is built from c_a / h_a.  Per tile: the three sums and the pair count.
+__global__ void __launch_bounds__(256)
+k_mp_spacing(const FTile *__restrict__ tiles, const int *__restrict__ perm,
+             const double *__restrict__ cent, ll nel, const unsigned *__restrict__ ell,
+             const ll *__restrict__ slice_off, const int *__restrict__ slice_w, unsigned wface,
+             double *__restrict__ part) {
+  const FTile t = tiles[blockIdx.x];
+  double s[4] = {0, 0, 0, 0};
+  for (ll i = t.b + threadIdx.x; i < t.e; i += blockDim.x) {
+    const int e = perm[i];
+    const ll sl = i >> 5;
+    const unsigned *ep = ell + slice_off[sl] + (i & 31);
+    const int wd = slice_w[sl];
+    for (int k = 0; k < wd; k++) {
+      const unsigned x = ep[(ll)k * 32];
+      if ((x >> 28) != wface) continue;
+      const int f = perm[x & 0x0FFFFFFFu];
+      for (int a = 0; a < 3; a++) {
+        const double d = cent[(ll)a * nel + e] - cent[(ll)a * nel + f];
+        s[a] += d * d;
+      }
+      s[3] += 1.0;
+    }
+  }
+  __shared__ double sh[32];
+  for (int q = 0; q < 4; q++) {
+    const double v = mp_block_sum(s[q], sh);
+    if (threadIdx.x == 0) part[(ll)blockIdx.x * 4 + q] = v;
+    __syncthreads();
+  }
+}
+
+// sa[g][a] = 1 / h_a (1 where an axis has no spacing: 2D z, no pairs)
+__global__ void k_mp_scales(const double *__restrict__ part, const int *__restrict__ tile0,
+                            const int *__restrict__ ntile, int ngroups,
+                            double *__restrict__ sa) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  double s[4] = {0, 0, 0, 0};
+  for (int t = tile0[g]; t < tile0[g] + ntile[g]; t++)
+    for (int q = 0; q < 4; q++) s[q] += part[(ll)t * 4 + q];
+  for (int a = 0; a < 3; a++) {
+    const double h2 = s[3] > 0.0 ? s[a] / s[3] : 0.0;
+    sa[(ll)g * 3 + a] = h2 > 0.0 ? 1.0 / sqrt(h2) : 1.0;
+  }
+}
+
 // per tile: sum of (c - o), sum of (c - o)(c - o)^T (6) about the group's
-// origin o = centroid of its first position (numerically safe raw moments)
+// origin o = centroid of its first position (numerically safe raw moments),
+// coordinates in element spacings
 __global__ void __launch_bounds__(256)
 k_mp_moments(const FTile *__restrict__ tiles, const ll *__restrict__ gstart,
              const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
-             double *__restrict__ part) {
+             const double *__restrict__ sa, double *__restrict__ part) {
   const FTile t = tiles[blockIdx.x];
   const int e0 = perm[gstart[t.g]];
   const double o[3] = {cent[e0], cent[nel + e0], cent[2 * nel + e0]};
+  const double *k = sa + (ll)t.g * 3;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (ll i = t.b + threadIdx.x; i < t.e; i += blockDim.x) {
     const int e = perm[i];
-    const double x = cent[e] - o[0], y = cent[nel + e] - o[1], z = cent[2 * nel + e] - o[2];
+    const double x = (cent[e] - o[0]) * k[0], y = (cent[nel + e] - o[1]) * k[1],
+                 z = (cent[2 * nel + e] - o[2]) * k[2];
     s[0] += x, s[1] += y, s[2] += z;
     s[3] += x * x, s[4] += y * y, s[5] += z * z;
     s[6] += x * y, s[7] += x * z, s[8] += y * z;
@@ -198,13 +254,14 @@ __device__ void jacobi3(double A[3][3], double d[3], double V[3][3]) {
 // first axis is taken inside their plane along the coordinate axis of
 // largest variance (the axis RCB would cut), so that a nearly degenerate
 // group gets the cut direction the reference's own start vector favours.
-// frame[g] = {mu[3], R[3][3] (rows = axes), 1/s}.
+// frame[g] = {mu[3], R[3][3] (rows = axes), 1/s, sa[3]}: mu in element
+// spacings, x~ = R (c * sa - mu) / s.
 __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__restrict__ part,
                             const int *__restrict__ tile0, const int *__restrict__ ntile,
                             const ll *__restrict__ gstart, const ll *__restrict__ gn,
                             const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
-                            int ngroups, int ndim, double *__restrict__ frame,
-                            int *__restrict__ degen) {
+                            int ngroups, int ndim, const double *__restrict__ sa,
+                            double *__restrict__ frame, int *__restrict__ degen) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngroups) return;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -212,7 +269,8 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
     for (int q = 0; q < 9; q++) s[q] += part[(ll)t * 9 + q];
   const double n = (double)gn[g];
   const int e0 = perm[gstart[g]];
-  const double o[3] = {cent[e0], cent[nel + e0], cent[2 * nel + e0]};
+  const double *k = sa + (ll)g * 3;
+  const double o[3] = {cent[e0] * k[0], cent[nel + e0] * k[1], cent[2 * nel + e0] * k[2]};
   double m[3] = {s[0] / n, s[1] / n, s[2] / n};
   double A[3][3];
   A[0][0] = s[3] - n * m[0] * m[0];
@@ -263,11 +321,20 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
   }
   const double var = l1 > 0.0 ? l1 / n : 0.0;
   const double inv_s = var > 0.0 ? 1.0 / sqrt(3.0 * var) : 0.0;
-  double *f = frame + (ll)g * 13;
-  for (int k = 0; k < 3; k++) f[k] = o[k] + m[k];
+  double *f = frame + (ll)g * MP_FRAME;
+  for (int q = 0; q < 3; q++) f[q] = o[q] + m[q];
   for (int a = 0; a < 3; a++)
-    for (int k = 0; k < 3; k++) f[3 + 3 * a + k] = R[a][k];
+    for (int q = 0; q < 3; q++) f[3 + 3 * a + q] = R[a][q];
   f[12] = inv_s;
+  for (int q = 0; q < 3; q++) f[13 + q] = k[q];
+}
+
+// x~ of element e in frame f (3 values)
+__device__ __forceinline__ void frame_coords(const double *f, const double *cent, ll nel, int e,
+                                             double out[3]) {
+  const double x = cent[e] * f[13] - f[0], y = cent[nel + e] * f[14] - f[1],
+               z = cent[2 * nel + e] * f[15] - f[2];
+  for (int a = 0; a < 3; a++) out[a] = (f[3 + 3 * a] * x + f[4 + 3 * a] * y + f[5 + 3 * a] * z) * f[12];
 }
 
 // Input features of every position: X[i] = (x~ (3), deg / 56, g, 0, 0, 0)
@@ -288,10 +355,10 @@ __global__ void k_mp_features(const int *__restrict__ perm, const int *__restric
   const int g = i < N ? grp[i] : -1;
   if (g >= 0) {
     const int e = perm[i];
-    const double *f = frame + (ll)g * 13;
-    const double x = cent[e] - f[0], y = cent[nel + e] - f[1], z = cent[2 * nel + e] - f[2];
-    for (int a = 0; a < 3; a++)
-      v[a] = (float)((f[3 + 3 * a] * x + f[4 + 3 * a] * y + f[5 + 3 * a] * z) * f[12]);
+    const double *f = frame + (ll)g * MP_FRAME;
+    double xt[3];
+    frame_coords(f, cent, nel, e, xt);
+    for (int a = 0; a < 3; a++) v[a] = (float)xt[a];
     const ll sl = i >> 5;
     const unsigned *ep = ell + slice_off[sl] + (i & 31);
     const int wd = slice_w[sl];
@@ -301,8 +368,7 @@ __global__ void k_mp_features(const int *__restrict__ perm, const int *__restric
     v[3] = (float)((double)acc * MP_DEG_SCALE);
     // the geometric guess -sin(pi x~_1 / 2) (the Fiedler vector of a uniform
     // bar along the first axis): an input, and the start the head corrects
-    const double t = (f[3] * x + f[4] * y + f[5] * z) * f[12];
-    v[4] = (float)(-sin(1.5707963267948966 * t));
+    v[4] = (float)(-sin(1.5707963267948966 * xt[0]));
   }
   float4 *o = reinterpret_cast<float4 *>(X + i * MP_FIN);
   o[0] = make_float4(v[0], v[1], v[2], v[3]);
@@ -844,10 +910,9 @@ __global__ void k_mp_geometric(const int *__restrict__ perm, const int *__restri
   double v = 0.0;
   if (g >= 0) {
     const int e = perm[i];
-    const double *f = frame + (ll)g * 13;
-    const double x = cent[e] - f[0], yy = cent[nel + e] - f[1], z = cent[2 * nel + e] - f[2];
-    const double t = (f[3] * x + f[4] * yy + f[5] * z) * f[12];
-    v = -sin(1.5707963267948966 * t);
+    double xt[3];
+    frame_coords(frame + (ll)g * MP_FRAME, cent, nel, e, xt);
+    v = -sin(1.5707963267948966 * xt[0]);
   }
   y[i] = v;
 }
@@ -917,8 +982,9 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
       tiles.push_back({b, std::min(b + MP_FTILE, v.gstart[g] + v.gn[g]), g});
     nt[g] = (int)tiles.size() - t0[g];
   }
-  frame.ensure((size_t)std::max(G, 1) * 13);
+  frame.ensure((size_t)std::max(G, 1) * MP_FRAME);
   DBuf<int> dg((size_t)std::max(G, 1));
+  DBuf<double> sa((size_t)std::max(G, 1) * 3);
   if (G > 0 && !tiles.empty()) {
     DBuf<FTile> dt(tiles.size());
     DBuf<int> d0(G), dn(G);
@@ -929,10 +995,18 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     h2d(gs.p, v.gstart.data(), G);
     h2d(gn.p, v.gn.data(), G);
     DBuf<double> part(tiles.size() * 9);
-    k_mp_moments<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, gs.p, v.perm, cent, nel, part.p);
+    const unsigned wface = ndim == 3 ? 4u : 2u;  // face (3D) or edge (2D) neighbours
+    k_mp_spacing<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, v.perm, cent, nel, v.lv->ell.p,
+                                                        v.lv->slice_off.p, v.lv->slice_w.p,
+                                                        wface, part.p);
+    CK_LAUNCH();
+    k_mp_scales<<<grid_for(G, 128), 128, 0, st>>>(part.p, d0.p, dn.p, G, sa.p);
+    CK_LAUNCH();
+    k_mp_moments<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, gs.p, v.perm, cent, nel, sa.p,
+                                                        part.p);
     CK_LAUNCH();
     k_mp_frames<<<grid_for(G, 128), 128, 0, st>>>(dt.p, part.p, d0.p, dn.p, gs.p, gn.p, v.perm,
-                                                  cent, nel, G, ndim, frame.p, dg.p);
+                                                  cent, nel, G, ndim, sa.p, frame.p, dg.p);
     CK_LAUNCH();
   }
   if (degen) {

@@ -53,7 +53,7 @@ def test_features_match_restatement():
     X = b.features().cpu().numpy().astype(np.float64)
     b.close()
     rows, col, w = _graph(vtx, group)
-    Xo = W.features(O.centroids(xyz, 8), group.astype(np.int64), rows, w)
+    Xo = W.features(O.centroids(xyz, 8), group.astype(np.int64), rows, col, w)
     # FP32 features computed in FP64 (Jacobi frames on the GPU, LAPACK here)
     np.testing.assert_allclose(X[:, :5], Xo[:, :5], rtol=1e-5, atol=1e-6)
     assert np.all(X[:, 5:] == 0)

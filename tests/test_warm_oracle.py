@@ -37,7 +37,7 @@ def test_features_axis_aligned_box():
     cent = O.centroids(xyz, 8)
     group = np.zeros(len(vtx), np.int64)
     rows, col, w = _graph(vtx, group)
-    X = W.features(cent, group, rows, w)
+    X = W.features(cent, group, rows, col, w)
     assert np.allclose(np.abs(X[:, 0]).max(), 11 / 12 * np.sqrt(12 ** 2 / (12 ** 2 - 1)), rtol=1e-9)
     assert np.all(np.diff(X[:12, 0]) > 0)  # x increases along the first row
     assert np.isclose(X[:, 3].max(), 1.0)
@@ -51,7 +51,7 @@ def test_gradient_matches_finite_differences():
     cent = O.centroids(xyz, 8)
     group = seg.astype(np.int64)
     rows, col, w = _graph(vtx, group)
-    X = W.features(cent, group, rows, w)
+    X = W.features(cent, group, rows, col, w)
     rng = np.random.default_rng(1)
     label = rng.normal(size=len(vtx))
     p = _params(2)
