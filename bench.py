@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--shape", default=None, help="override mesh shape nx,ny,nz")
     ap.add_argument("--nparts", type=int, default=None)
     ap.add_argument("--fp32", type=int, default=None)
+    ap.add_argument("--method", default="warm", choices=["warm", "reference"],
+                    help="warm: geometric warm start + residual stop; reference: the "
+                         "reference's start vector and stopping rule")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-plain", action="store_true",
@@ -340,8 +343,18 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     # the named method: FP32 vectors on exact integer weights, FP64 dots and
-    # eigensolve (--fp32 0 runs every vector in FP64)
+    # eigensolve (--fp32 0 runs every vector in FP64); warm start: the
+    # geometric guess per group, judged against the reference's step start
+    # (groups with two nearly equal axes keep the step start); batched: all
+    # groups of a level per launch; Lanczos restarts until every Fiedler
+    # vector's FP64 eigen-residual is at most rsb_tol (--method reference:
+    # the reference's start vector and stopping rule)
     os.environ["PARRSB_GPU_FP32"] = str(1 if args.fp32 is None else args.fp32)
+    method_env = ({"PARRSB_GPU_START": "2", "PARRSB_GPU_RESID_STOP": "1"}
+                  if args.method == "warm" else
+                  {"PARRSB_GPU_START": "0", "PARRSB_GPU_RESID_STOP": "0"})
+    method_env.update({"PARRSB_GPU_WARM": "0", "PARRSB_GPU_WARM_MIN": "0"})
+    os.environ.update(method_env)
     os.environ.setdefault("PARRSB_VERBOSE_LEVEL", "0")
     import parrsb_gb300 as P
     from parrsb_gb300 import meshgen
@@ -460,17 +473,25 @@ def main():
         part = d_part.cpu().numpy()
     q = P.part_quality(part, vtx, nparts)
     # ---- plain GPU path: every group of a level solved by its own launches
+    # ---- the plain GPU path: the reference's start vector, every group of a
+    # level solved by its own launches (no batching, no graphs), the same
+    # tolerance and stopping rule
     plain = None
     if not args.no_plain:
         os.environ["PARRSB_GPU_BATCHED"] = "0"
+        os.environ["PARRSB_GPU_START"] = "0"
         barrier()
         tp0 = time.perf_counter()
         sp = step_device()
         barrier()
         plain = {"value": max_over_ranks(time.perf_counter() - tp0), "unit": "s",
-                 "what": "one step with per-group Lanczos launches (no batching, no graphs)",
+                 "what": ("one step with the reference's start vector and per-group Lanczos "
+                          "launches (no batching, no graphs), same stopping rule"),
                  "lanczos_steps": int(sp.lanczos_iters),
+                 "max_fiedler_resid": sp.max_fiedler_resid,
+                 "weighted_cut": P.part_quality(d_part.cpu().numpy(), vtx, nparts)[0],
                  "kernel_launches": int(sp.kernel_launches)}
+        os.environ.update(method_env)
         os.environ["PARRSB_GPU_BATCHED"] = "1"
 
     # ---- the same step with FP64 vectors: time and the error of the mixed path
@@ -481,17 +502,17 @@ def main():
     starts = None
     if not args.no_plain:
         starts = {}
-        RS = {"PARRSB_GPU_RESID_STOP": "1"}
-        legs = [("reference_start", {}), ("random_start", {"PARRSB_GPU_START": "1"}),
-                ("geometric_start", {"PARRSB_GPU_START": "2"}),
-                ("reference_start_resid_stop", dict(RS)),
-                ("geometric_start_resid_stop", dict(RS, PARRSB_GPU_START="2"))]
+        def leg(start, stop, warm=0, warm_min=0):
+            return {"PARRSB_GPU_START": str(start), "PARRSB_GPU_RESID_STOP": str(stop),
+                    "PARRSB_GPU_WARM": str(warm), "PARRSB_GPU_WARM_MIN": str(warm_min)}
+        legs = [("reference_start", leg(0, 0)), ("random_start", leg(1, 0)),
+                ("geometric_start", leg(2, 0)),
+                ("reference_start_resid_stop", leg(0, 1)),
+                ("geometric_start_resid_stop", leg(2, 1))]
         if warm_ok:
-            legs += [("learned_start", {"PARRSB_GPU_WARM": "1"}),
-                     ("learned_start_resid_stop", dict(RS, PARRSB_GPU_WARM="1")),
-                     ("learned_1M_geometric_resid_stop",
-                      dict(RS, PARRSB_GPU_WARM="1", PARRSB_GPU_START="2",
-                           PARRSB_GPU_WARM_MIN="1048576"))]
+            legs += [("learned_start", leg(0, 0, 1)),
+                     ("learned_start_resid_stop", leg(0, 1, 1)),
+                     ("learned_1M_geometric_resid_stop", leg(2, 1, 1, 1 << 20))]
         for name, env in legs:
             saved = {k: os.environ.get(k) for k in env}
             os.environ.update(env)
@@ -581,7 +602,17 @@ def main():
         "data": "synthetic",
         "config": workload_config(shape, nparts),
         "method": {"batched": "all groups of a level per launch, one CUDA graph per pass",
-                   "parallelism": f"replicas x{world}"},
+                   "start": ("geometric warm start -sin(pi x1/2) along each group's principal "
+                             "axis in element spacings, judged per group against the "
+                             "reference's step start by FP64 eigen-residual; groups with two "
+                             "axes within 5% keep the step start"
+                             if args.method == "warm" else "the reference's step start"),
+                   "stop": ("restart until the FP64 eigen-residual <= rsb_tol"
+                            if args.method == "warm" else
+                            "the reference's CG-residual rule"),
+                   "learned_start": "see start_vectors.learned_* (network inference cost "
+                                    "included)",
+                   "env": method_env, "parallelism": f"replicas x{world}"},
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(part.nbytes), "last_call": e2e_stages,
                 "link": link},
