@@ -286,7 +286,7 @@ def _time_device(fn, reps=3):
     return best
 
 
-def other_rows(P, meshgen, lib, torch, ctypes):
+def other_rows(P, meshgen, lib, torch, ctypes, np):
     """RCB / RIB of the 512x512 quad annulus (262,144 elements) to 1024 parts,
     gencon on the same annulus (the reference algorithm's element check
     fails there) and on a 128x128x64 jittered hex box (8.4M corner points);
@@ -314,6 +314,23 @@ def other_rows(P, meshgen, lib, torch, ctypes):
     t = _time_device(gc2)
     out["gencon_annulus_512x512"] = {"s": t, "return_code": 1,
                                      "distinct_ids": int(P.last_stats().gencon_segments)}
+    # batched level solve: 4,096 subgraphs (200-20,000 elements, 5% deleted),
+    # the Fiedler vector of every one: one segmented launch sequence per
+    # Lanczos pass (CUDA graph) against one subgraph at a time
+    vc, _, sc = meshgen.subboxes(4096, smin=200, smax=20000, delete=0.05, seed=0)
+    c4 = {"subgraphs": 4096, "elements": int(len(vc))}
+    for mode, batched in (("segmented", True), ("per_subgraph", False)):
+        P.fiedler_groups(vc[:50000], sc[:50000], int(sc[49999]) + 1, batched=batched)  # warm-up
+        t = time.perf_counter()
+        f, it, rs = P.fiedler_groups(vc, sc, 4096, batched=batched)
+        st = P.last_stats()
+        c4[mode] = {"s": time.perf_counter() - t, "lanczos_steps": int(it.sum()),
+                    "kernel_launches": int(st.kernel_launches),
+                    "max_resid_connected_p99": float(np.percentile(rs, 99))}
+    c4["segmented_speedup"] = c4["per_subgraph"]["s"] / c4["segmented"]["s"]
+    c4["components_max"] = int(P.components(vc, sc, 4096).max())
+    out["c4_batched_level_solve"] = c4
+    del vc, sc
     _, xyz3 = meshgen.box_hex(128, 128, 64, jitter=0.1, seed=0)
     d3 = torch.from_numpy(xyz3).cuda()
     ids3 = torch.empty(xyz3.shape[0] * 8, dtype=torch.int64, device="cuda")
@@ -560,7 +577,7 @@ def main():
 
     extras = None
     if not args.no_extras and rank == 0:
-        extras = other_rows(P, meshgen, lib, torch, ctypes)
+        extras = other_rows(P, meshgen, lib, torch, ctypes, np)
 
     s = stats[-1]
     spmv_ms = sum(x.spmv_ms for x in stats)
