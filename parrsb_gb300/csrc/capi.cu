@@ -72,9 +72,10 @@ namespace {
 
 struct Workspace {
   GenconWs gc;
-  DBuf<long long> vtx;
-  DBuf<double> xyz, cent;
-  DBuf<int> part;
+  PBuf<long long> vtx;  // host inputs land here (cudaMalloc, kept across calls)
+  PBuf<double> xyz;
+  DBuf<double> cent;
+  PBuf<int> part;
   DBuf<long long> ids;
 };
 // per thread and device: buffers cached by earlier calls on the device that
@@ -140,6 +141,11 @@ void print_options(const parrsb_options *o) {
   print_if(v, "PARRSB_RSB_TOL = %lf", o->rsb_tol);
   print_if(v, "PARRSB_RSB_MG_GRAMMIAN = %d", o->rsb_mg_grammian);
   print_if(v, "PARRSB_RSB_MG_FACTOR = %d", o->rsb_mg_factor);
+}
+
+double env_double(const char *name, double def) {
+  const char *v = getenv(name);
+  return v ? atof(v) : def;
 }
 
 int env_int(const char *name, int def) {
@@ -291,6 +297,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.warm = env_int("PARRSB_GPU_WARM", 0);
     ro.warm_min = env_int("PARRSB_GPU_WARM_MIN", 0);
     ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
+    ro.cg_factor = env_double("PARRSB_GPU_RESID_CG_FACTOR", 1.0);
     if (ro.warm) load_warm_weights_from_env();
     rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq, sg);
     sync();
@@ -603,6 +610,7 @@ extern "C" int parrsb_fiedler_groups(double *fiedler, long long *iters, double *
       ro.batched = batched ? 1 : 0;
       ro.start = env_int("PARRSB_GPU_START", 0);
       ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
+      ro.cg_factor = env_double("PARRSB_GPU_RESID_CG_FACTOR", 1.0);
       fiedler_groups_device(dv.p, N, nv, dg.p, ngroups, ro, df.p, it.data(), rs.data());
       d2h(fiedler, df.p, (size_t)N);
       sync();

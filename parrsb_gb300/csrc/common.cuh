@@ -84,6 +84,31 @@ struct DBuf {
   T *get() const { return p; }
 };
 
+// Device buffer that lives across calls (the cached upload / download
+// buffers of the host entry points): plain cudaMalloc / cudaFree instead of
+// the stream-ordered pool, so that the pool's growth and reuse by the
+// temporaries of a call never touch the pages the host copies land in.
+template <typename T>
+struct PBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  PBuf() {}
+  PBuf(const PBuf &) = delete;
+  PBuf &operator=(const PBuf &) = delete;
+  void ensure(size_t count) {
+    if (count == 0) count = 1;
+    if (p && count <= n) return;
+    release();
+    CK(cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr, n = 0;
+  }
+  ~PBuf() { release(); }
+};
+
 // One per host thread.  Every call runs on the device that is current when
 // it starts: init() selects that device's stream (created on first use) and
 // workspace, so a thread may switch devices between calls.

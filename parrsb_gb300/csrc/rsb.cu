@@ -1476,6 +1476,8 @@ struct Lanczos {
   bool sp_fused = false;
   int ritz_bd = 256;             // threads per block of k_ritz
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
+  double resid_tol = 0.0;        // its bound (rsb_tol); passes then use
+  double cg_factor = 1.0;        //   tol * cg_factor for their own CG exit
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
 
   void setup(const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N_, int miter) {
@@ -1704,7 +1706,7 @@ struct Lanczos {
       tile<TM_RESID1, GATE_ACTIVE>(0, &lv);
       fin<FIN_RESID1, GATE_ACTIVE>();
       tile<TM_RESID2, GATE_ACTIVE>(0, &lv);
-      fin<FIN_RESID_GATE, GATE_ACTIVE>(0, tol, mpass);
+      fin<FIN_RESID_GATE, GATE_ACTIVE>(0, resid_tol, mpass);
     }
   }
 
@@ -1789,7 +1791,11 @@ struct Lanczos {
   void run(const Level &lv, double tol, int mpass, bool use_graph, bool warm,
            int start_kind = 0) {
     cudaStream_t st = ctx().stream;
-    if (resid_stop) y64.ensure((size_t)N);
+    if (resid_stop) {
+      y64.ensure((size_t)N);
+      resid_tol = tol;
+      tol = tol * cg_factor;  // a pass's own CG exit
+    }
     // the vectors are scratch until the first pass initialises them
     CK(cudaMemsetAsync(p.p, 0, (size_t)N * sizeof(VT), st));
     if (eig_smem() > 48 * 1024)
@@ -2270,6 +2276,7 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
                        const double *y_warm = nullptr, const std::vector<int> &degen = {}) {
   lz.setup(gstart, gn, N, o.miter);
   lz.resid_stop = o.resid_stop != 0;
+  lz.cg_factor = o.cg_factor;
   {
     StageTimer tm(PARRSB_STAGE_LANCZOS);
     if (y_warm) lz.choose_start(lv, y_warm, o.start, degen);

@@ -56,6 +56,8 @@ struct RsbOpts {
   // 1 also restart until the Ritz vector's FP64 eigen-residual
   // ||L f - rho f|| / ||f|| is at most tol (or mpass restarts).
   int resid_stop = 0;
+  // with resid_stop: a restart's own CG exit at tol * cg_factor
+  double cg_factor = 1.0;
 };
 
 // Starting point of a recursion other than one group of all elements:
