@@ -319,15 +319,20 @@ def other_rows(P, meshgen, lib, torch, ctypes, np):
     # Lanczos pass (CUDA graph) against one subgraph at a time
     vc, _, sc = meshgen.subboxes(4096, smin=200, smax=20000, delete=0.05, seed=0)
     c4 = {"subgraphs": 4096, "elements": int(len(vc))}
-    for mode, batched in (("segmented", True), ("per_subgraph", False)):
+    n512 = int(np.searchsorted(sc, 512))
+    for mode, batched, ng in (("segmented", True, 4096), ("segmented_first_512", True, 512),
+                              ("per_subgraph_first_512", False, 512)):
+        n = len(vc) if ng == 4096 else n512
         P.fiedler_groups(vc[:50000], sc[:50000], int(sc[49999]) + 1, batched=batched)  # warm-up
         t = time.perf_counter()
-        f, it, rs = P.fiedler_groups(vc, sc, 4096, batched=batched)
+        f, it, rs = P.fiedler_groups(vc[:n], sc[:n], ng, batched=batched)
         st = P.last_stats()
-        c4[mode] = {"s": time.perf_counter() - t, "lanczos_steps": int(it.sum()),
+        c4[mode] = {"s": time.perf_counter() - t, "elements": n, "lanczos_steps": int(it.sum()),
                     "kernel_launches": int(st.kernel_launches),
-                    "max_resid_connected_p99": float(np.percentile(rs, 99))}
-    c4["segmented_speedup"] = c4["per_subgraph"]["s"] / c4["segmented"]["s"]
+                    "resid_p99": float(np.percentile(rs, 99)), "resid_max": float(rs.max()),
+                    "above_tol": int((rs > 1e-5).sum())}
+    c4["segmented_speedup_first_512"] = (c4["per_subgraph_first_512"]["s"] /
+                                         c4["segmented_first_512"]["s"])
     c4["components_max"] = int(P.components(vc, sc, 4096).max())
     out["c4_batched_level_solve"] = c4
     del vc, sc

@@ -261,6 +261,8 @@ struct GState {
   ll total_iters;
   int tile0, ntiles, miter, run, iters, done, active, npass;
   int warm;  // start from the learned prediction (else the fallback start)
+  int stall;          // residual-stop mode: restarts in a row without progress
+  double prev_resid;  //   and the residual of the restart before
 };
 
 __device__ __forceinline__ double block_sum(double v, double *sh) {
@@ -397,8 +399,13 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     s.npass += 1;
     atomicMax(any_active + 1, s.iters);  // active stays set until FIN_RESID_GATE
   } else if (OP == FIN_RESID_GATE) {
+    // restart while the residual is above tol, at most mpass restarts, and
+    // stop after three restarts in a row that did not lower it by 10% (the
+    // vector has reached what the working precision allows)
     s.resid = __ddiv_rn(__dsqrt_rn(tot[0]), __dsqrt_rn(s.ff));
-    s.active = (!(s.resid <= tol) && s.npass < mpass) ? 1 : 0;
+    if (s.resid > 0.9 * s.prev_resid) s.stall += 1; else s.stall = 0;
+    s.prev_resid = s.resid;
+    s.active = (!(s.resid <= tol) && s.npass < mpass && s.stall < 3) ? 1 : 0;
     if (s.active) atomicOr(any_active, 1);
   } else if (OP == FIN_NORM) {
     s.c = __ddiv_rn(1.0, __dsqrt_rn(tot[0]));
@@ -1435,6 +1442,8 @@ __global__ void k_set_active(GState *__restrict__ gs, int ngroups) {
     gs[g].npass = 0;
     gs[g].total_iters = 0;
     gs[g].run = 0;
+    gs[g].stall = 0;
+    gs[g].prev_resid = 1e300;
   }
 }
 

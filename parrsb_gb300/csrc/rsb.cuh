@@ -56,8 +56,10 @@ struct RsbOpts {
   // 1 also restart until the Ritz vector's FP64 eigen-residual
   // ||L f - rho f|| / ||f|| is at most tol (or mpass restarts).
   int resid_stop = 0;
-  // with resid_stop: a restart's own CG exit at tol * cg_factor
-  double cg_factor = 1.0;
+  // with resid_stop: a restart's own CG exit at tol * cg_factor (a tighter
+  // exit makes every restart count: at the same tol restarts end after a
+  // step or two once the vector is close, without improving it)
+  double cg_factor = 0.1;
 };
 
 // Starting point of a recursion other than one group of all elements:
