@@ -530,13 +530,16 @@ def main():
     starts = None
     if not args.no_plain:
         starts = {}
-        def leg(start, stop, warm=0, warm_min=0):
+        def leg(start, stop, warm=0, warm_min=0, reorth=0):
             return {"PARRSB_GPU_START": str(start), "PARRSB_GPU_RESID_STOP": str(stop),
-                    "PARRSB_GPU_WARM": str(warm), "PARRSB_GPU_WARM_MIN": str(warm_min)}
+                    "PARRSB_GPU_WARM": str(warm), "PARRSB_GPU_WARM_MIN": str(warm_min),
+                    "PARRSB_GPU_REORTH": str(reorth)}
         legs = [("reference_start", leg(0, 0)), ("random_start", leg(1, 0)),
                 ("geometric_start", leg(2, 0)),
                 ("reference_start_resid_stop", leg(0, 1)),
-                ("geometric_start_resid_stop", leg(2, 1))]
+                ("geometric_start_resid_stop", leg(2, 1)),
+                ("geometric_start_resid_stop_reorth", leg(2, 1, reorth=1)),
+                ("reference_start_reorth", leg(0, 0, reorth=1))]
         if warm_ok:
             legs += [("learned_start", leg(0, 0, 1)),
                      ("learned_start_resid_stop", leg(0, 1, 1)),

@@ -298,6 +298,7 @@ void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int
     ro.warm_min = env_int("PARRSB_GPU_WARM_MIN", 0);
     ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
     ro.cg_factor = env_double("PARRSB_GPU_RESID_CG_FACTOR", 0.1);
+    ro.reorth = env_int("PARRSB_GPU_REORTH", 0);
     if (ro.warm) load_warm_weights_from_env();
     rsb_device(d_vtx, W.cent.p, N, nv, P, ro, d_part, d_seq, sg);
     sync();
@@ -611,6 +612,7 @@ extern "C" int parrsb_fiedler_groups(double *fiedler, long long *iters, double *
       ro.start = env_int("PARRSB_GPU_START", 0);
       ro.resid_stop = env_int("PARRSB_GPU_RESID_STOP", 0);
       ro.cg_factor = env_double("PARRSB_GPU_RESID_CG_FACTOR", 0.1);
+      ro.reorth = env_int("PARRSB_GPU_REORTH", 0);
       fiedler_groups_device(dv.p, N, nv, dg.p, ngroups, ro, df.p, it.data(), rs.data());
       d2h(fiedler, df.p, (size_t)N);
       sync();

@@ -1230,6 +1230,114 @@ k_ritz(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Reorthogonalisation (opt-in, PARRSB_GPU_REORTH=1).  The reference keeps
+// the Krylov basis orthogonal only to the constant vector (ortho,
+// src/fiedler.c:20-30, 470); in finite precision the residuals r_0 .. r_k
+// (rows of V) lose their mutual orthogonality as Ritz values converge.
+// Here every new residual is orthogonalised against all earlier ones by
+// classical Gram-Schmidt with FP64 coefficients:
+//   r_{k+1} <- r_{k+1} - sum_j (r_j . r_{k+1} / |r_j|^2) r_j,
+// before its norm enters the recurrence (beta, the stopping test, T).
+// k_rdot: tile partials of d_j = r_j . r_{k+1}; each thread keeps its rows
+// of r_{k+1} in registers (at most 32: tiles of at most 8192 rows and 256
+// threads), sums its products in the vector type and the block adds the
+// threads' sums in a fixed order (FP64).
+// ---------------------------------------------------------------------------
+constexpr int RO_THREADS = 256;
+constexpr int RO_ROWS = LZ_TILE / RO_THREADS;  // 32
+
+template <typename VT>
+__global__ void __launch_bounds__(RO_THREADS)
+k_rdot(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+       const GState *__restrict__ gs, const VT *__restrict__ V, ll VS, int it, int MI,
+       double *__restrict__ part2) {
+  pdl_entry();
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
+  if (!gs[g].run) return;
+  const ll b = tbeg[t], e = tend[t];
+  const VT *__restrict__ rn = V + (ll)(it + 1) * VS;
+  VT x[RO_ROWS];
+#pragma unroll
+  for (int q = 0; q < RO_ROWS; q++) {
+    const ll i = b + threadIdx.x + (ll)q * RO_THREADS;
+    x[q] = i < e ? rn[i] : (VT)0;
+  }
+  __shared__ double sh[RO_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = 0; j <= it; j++) {
+    const VT *__restrict__ rj = V + (ll)j * VS;
+    VT acc = (VT)0;
+#pragma unroll
+    for (int q = 0; q < RO_ROWS; q++) {
+      const ll i = b + threadIdx.x + (ll)q * RO_THREADS;
+      if (i < e) acc = acc + x[q] * rj[i];
+    }
+    double v = warp_tree_sum((double)acc);
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int w = 0; w < RO_THREADS / 32; w++) s = __dadd_rn(s, sh[w]);
+      part2[(ll)t * (MI + 1) + j] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// One block per group: h_j = (sum over the group's tiles, in order, of d_j)
+// / |r_j|^2 (vnorm holds |r_j|).
+__global__ void k_rdot_fin(const GState *__restrict__ gs, int ngroups,
+                           const double *__restrict__ part2, const double *__restrict__ vnorm,
+                           int it, int MI, double *__restrict__ h) {
+  pdl_entry();
+  const int g = blockIdx.x;
+  if (g >= ngroups) return;
+  const GState &s = gs[g];
+  if (!s.run) return;
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) {
+    double d = 0.0;
+    for (int q = 0; q < s.ntiles; q++) d = __dadd_rn(d, part2[(ll)(s.tile0 + q) * (MI + 1) + j]);
+    const double nj = vnorm[(ll)g * (MI + 1) + j];
+    h[(ll)g * (MI + 1) + j] = nj > 0.0 ? __ddiv_rn(d, __dmul_rn(nj, nj)) : 0.0;
+  }
+}
+
+// r_{k+1} -= sum_j h_j r_j, and the tile partial of |r_{k+1}|^2 (for the
+// recurrence's finalisation, in place of the plain update's).
+template <typename VT>
+__global__ void __launch_bounds__(RO_THREADS)
+k_rupd(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+       const GState *__restrict__ gs, VT *__restrict__ V, ll VS, int it, int MI,
+       const double *__restrict__ h, double *__restrict__ part) {
+  pdl_entry();
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
+  if (!gs[g].run) return;
+  __shared__ VT hs[MAX_MITER + 1];
+  for (int j = threadIdx.x; j <= it; j += blockDim.x) hs[j] = (VT)h[(ll)g * (MI + 1) + j];
+  __syncthreads();
+  const ll b = tbeg[t], e = tend[t];
+  VT *__restrict__ rn = V + (ll)(it + 1) * VS;
+  double acc = 0.0;
+  for (ll i = b + threadIdx.x; i < e; i += RO_THREADS) {
+    VT v = rn[i];
+    for (int j = 0; j <= it; j++) v = v - hs[j] * V[(ll)j * VS + i];
+    rn[i] = v;
+    acc += (double)(v * v);
+  }
+  __shared__ double sh[RO_THREADS / 32];
+  const double w = warp_tree_sum(acc);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < RO_THREADS / 32; q++) s = __dadd_rn(s, sh[q]);
+    part[t] = s;
+  }
+}
+
 // Tridiagonal eigensolve for the Ritz vector, one warp per group.
 // GB300 runs long dependent FP64 chains slowly, so instead of the implicit
 // QL sweep of the reference (tqli, src/fiedler.c:328-432, about 2000
@@ -1485,6 +1593,8 @@ struct Lanczos {
   // the same choice for the SpMV (PARRSB_GPU_SPMV_FUSED=1: fused)
   bool sp_fused = false;
   int ritz_bd = 256;             // threads per block of k_ritz
+  bool reorth = false;           // reorthogonalise every residual (opt-in)
+  DBuf<double> part2, hro;       //   its tile partials and coefficients
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
   double resid_tol = 0.0;        // its bound (rsb_tol); passes then use
   double cg_factor = 1.0;        //   tol * cg_factor for their own CG exit
@@ -1688,13 +1798,20 @@ struct Lanczos {
       if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
       (*spmv_launches)++;
       mark(4 * it + 2);
-      if (pr_fused) {
+      if (pr_fused && !reorth) {
         launch_pdl(pr_u == 4 ? k_pr<VT, TM_R, 4> : k_pr<VT, TM_R, 1>, T, pr_bd, 0, st, tbeg.p,
                    tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p, fargs(it, tol, mpass));
       } else {
         launch_pdl(pr_u == 4 ? k_pr<VT, TM_R, 4, false> : k_pr<VT, TM_R, 1, false>, T, pr_bd, 0,
                    st, tbeg.p, tend.p, tgrp.p, gs.p, p.p, w.p, V.p, VS, part.p,
                    fargs(it, tol, mpass));
+        if (reorth) {  // against r_0 .. r_it; rewrites the partials of |r_{it+1}|^2
+          launch_pdl(k_rdot<VT>, T, RO_THREADS, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, V.p, VS, it,
+                     MI, part2.p);
+          launch_pdl(k_rdot_fin, A, 64, 0, st, gs.p, A, part2.p, vnorm.p, it, MI, hro.p);
+          launch_pdl(k_rupd<VT>, T, RO_THREADS, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, V.p, VS, it,
+                     MI, hro.p, part.p);
+        }
         fin<FIN_RTR, GATE_RUN>(it, tol, mpass);
       }
       mark(4 * it + 3);
@@ -1838,7 +1955,8 @@ struct Lanczos {
       CK(cudaGraphInstantiate(&exec, graph, 0));
     }
     const long long per_pass_kernels =
-        4 + (long long)MI * (pr_fused ? 3 : 5) + (sp_fused ? 0 : MI) + 5 + (resid_stop ? 4 : 0);
+        4 + (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) + 5 +
+        (resid_stop ? 4 : 0) + (reorth ? 3ll * MI : 0);
     launches = 0;
     // PARRSB_GPU_LEVEL_LOG=1 (timing mode): one line per level on stderr
     const bool level_log = !ev.empty() && getenv("PARRSB_GPU_LEVEL_LOG");
@@ -2285,6 +2403,11 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
                        double *f_pos, std::vector<GState> &res,
                        const double *y_warm = nullptr, const std::vector<int> &degen = {}) {
   lz.setup(gstart, gn, N, o.miter);
+  lz.reorth = o.reorth != 0;
+  if (lz.reorth) {
+    lz.part2.ensure((size_t)lz.T * (o.miter + 1) + 1);
+    lz.hro.ensure((size_t)lz.A * (o.miter + 1) + 1);
+  }
   lz.resid_stop = o.resid_stop != 0;
   lz.cg_factor = o.cg_factor;
   {

@@ -56,6 +56,9 @@ struct RsbOpts {
   // 1 also restart until the Ritz vector's FP64 eigen-residual
   // ||L f - rho f|| / ||f|| is at most tol (or mpass restarts).
   int resid_stop = 0;
+  // reorthogonalise every new Lanczos residual against the earlier ones
+  // (classical Gram-Schmidt, FP64 coefficients)
+  int reorth = 0;
   // with resid_stop: a restart's own CG exit at tol * cg_factor (a tighter
   // exit makes every restart count: at the same tol restarts end after a
   // step or two once the vector is close, without improving it)

@@ -190,3 +190,21 @@ def test_trained_network_gain(monkeypatch):
           f"restarts {cold.lanczos_passes} -> {hot.lanczos_passes}, start residual "
           f"{hot.start_resid_fallback:.3e} -> {hot.start_resid_warm:.3e}, "
           f"{hot.warm_used}/{hot.warm_tried} groups from the network")
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+@pytest.mark.parametrize("stop", ["0", "1"])
+def test_reorthogonalised_lanczos(oracle, monkeypatch, fp32, stop):
+    """PARRSB_GPU_REORTH=1: every new Lanczos residual is orthogonalised
+    against the earlier ones; the partition keeps the oracle's part sizes
+    and a cut within 1%, with both stopping rules."""
+    vtx, xyz = meshgen.box_hex(24, 20, 16, jitter=0.1, seed=2)
+    part, st = _rsb(vtx, xyz, 8, monkeypatch, PARRSB_GPU_REORTH=1, PARRSB_GPU_FP32=fp32,
+                    PARRSB_GPU_RESID_STOP=stop)
+    assert st.unconverged == 0
+    if stop == "1":
+        assert st.max_fiedler_resid <= 1e-5
+    rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, 8, partitioner=0)
+    np.testing.assert_array_equal(np.bincount(part, minlength=8), np.bincount(ref, minlength=8))
+    q, qr = oracle.part_quality(part, vtx, 8), oracle.part_quality(ref, vtx, 8)
+    assert abs(q[0] - qr[0]) <= 0.01 * qr[0]
