@@ -60,7 +60,9 @@ typedef struct {
   int tagged;                  /* tagged partitioning: tag[e] groups elements */
   int levels;                  /* 1 or 2; clamped to <= 2 (default 2) */
   int find_disconnected_comps; /* count components per bisection (1) */
-  int repair;                  /* accepted, no effect (as in the reference) */
+  int repair;                  /* 1: repair disconnected parts after the
+                                  partition (no counterpart in the reference,
+                                  which parses it and does nothing; 0) */
   int verbose_level;           /* 0 quiet, >=1 prints options and time (1) */
   int profile_level;           /* >=1 prints per-level stage times (0) */
   int rsb_algo;                /* 0 Lanczos (1 = multigrid: unsupported) */
@@ -170,6 +172,8 @@ typedef struct {
   double start_resid_fallback;/* geometric mean of the judged groups' start */
   double start_resid_warm;    /*   residuals: fallback and learned starts */
   long long level_steps[16];  /* Lanczos steps per bisection level (last: 15+) */
+  long long repair_components;/* repair = 1: components moved to another part */
+  long long repair_elements;  /*   and their elements */
 } parrsb_stats;
 
 enum {

@@ -258,3 +258,45 @@ def fiedler(vtx, miter=50, mpass=50, tol=1e-5):
     it = lib().oracle_fiedler(_p(f), _p(vtx), len(vtx), vtx.shape[1], miter,
                               mpass, tol)
     return f, it
+
+
+def repair_parts(part, vtx, nparts):
+    """Restatement of the library's repair of disconnected parts
+    (parrsb_options.repair = 1; the reference parses the option and does
+    nothing with it, src/parrsb.c:65): every part keeps its largest
+    vertex-connected component (ties: the one holding the part's smallest
+    element index); every other component moves, whole, to the part it
+    shares the largest dual-graph weight with (ties: smallest part number);
+    a component without a neighbour in another part stays.
+    Returns (new part, moved components, moved elements)."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    part = np.asarray(part, np.int64)
+    n = len(part)
+    rowptr, col, w = dual_graph(vtx)
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+    same = part[rows] == part[col]
+    A = coo_matrix((np.ones(int(same.sum())), (rows[same], col[same])), shape=(n, n))
+    ncomp, comp = connected_components(A, directed=False)
+    size = np.bincount(comp, minlength=ncomp)
+    first = np.full(ncomp, n, np.int64)
+    np.minimum.at(first, comp, np.arange(n))
+    cpart = part[first]
+    keep = {}
+    for c in np.lexsort((first, -size)):  # largest first, then smallest first element
+        keep.setdefault(int(cpart[c]), int(c))
+    out = part.copy()
+    moved_c = moved_e = 0
+    cross = ~same
+    for c in range(ncomp):
+        if keep[int(cpart[c])] == c:
+            continue
+        sel = cross & (comp[rows] == c)
+        if not sel.any():
+            continue
+        wsum = np.bincount(part[col[sel]], weights=w[sel], minlength=nparts)
+        tgt = int(np.argmax(wsum))  # first maximum: the smallest part
+        out[comp == c] = tgt
+        moved_c += 1
+        moved_e += int(size[c])
+    return out.astype(np.int32), moved_c, moved_e

@@ -63,7 +63,9 @@ class Stats(ctypes.Structure):
                 ("warm_ms", ctypes.c_double),
                 ("start_resid_fallback", ctypes.c_double),
                 ("start_resid_warm", ctypes.c_double),
-                ("level_steps", ctypes.c_longlong * 16)]
+                ("level_steps", ctypes.c_longlong * 16),
+                ("repair_components", ctypes.c_longlong),
+                ("repair_elements", ctypes.c_longlong)]
 
     def as_dict(self):
         d = {}

@@ -232,9 +232,28 @@ __global__ void k_seq_write(const int *__restrict__ perm, const int *__restrict_
   seq[e] = (int)(i - first[part[e]]);
 }
 
+void part_mesh_dev_impl(int *d_part, const long long *d_vtx, const double *d_xyz, int nel,
+                        int nv, const parrsb_options *o, int nparts, int *d_seq,
+                        const StartGroups *sg);
+
+// The partition, then (options->repair == 1, with vertex ids) the repair of
+// disconnected parts (repair.cu); the within-part order seq, if asked for,
+// is the order before the repair.
 void part_mesh_dev(int *d_part, const long long *d_vtx, const double *d_xyz, int nel, int nv,
                    const parrsb_options *o, int nparts, int *d_seq = nullptr,
                    const StartGroups *sg = nullptr) {
+  part_mesh_dev_impl(d_part, d_vtx, d_xyz, nel, nv, o, nparts, d_seq, sg);
+  if (o->repair == 1 && d_vtx && nel > 0) {
+    long long mc = 0, me = 0;
+    repair_parts_device(d_vtx, nel, nv, nparts, d_part, &mc, &me);
+    ctx().stats.repair_components = mc;
+    ctx().stats.repair_elements = me;
+  }
+}
+
+void part_mesh_dev_impl(int *d_part, const long long *d_vtx, const double *d_xyz, int nel,
+                        int nv, const parrsb_options *o, int nparts, int *d_seq,
+                        const StartGroups *sg) {
   cudaStream_t st = ctx().stream;
   if (nel == 0) return;
   int ndim = (nv == 8) ? 3 : 2;

@@ -2348,7 +2348,8 @@ void build_level(const Graph &g, const int *perm, const int *inv, const int *grp
 // tree; full rounds then visit only the rows outside the tree of hstart[h]
 // (PARRSB_GPU_CC_FULL=1: every row every round).  Returns the counts by id.
 std::vector<int> count_components_level(const Level &lv, const int *half, ll N,
-                                        const std::vector<ll> &hstart) {
+                                        const std::vector<ll> &hstart,
+                                        DBuf<int> *labels_out = nullptr) {
   cudaStream_t st = ctx().stream;
   const int nh = (int)hstart.size();
   std::vector<int> hc(nh, 0);
@@ -2392,6 +2393,7 @@ std::vector<int> count_components_level(const Level &lv, const int *half, ll N,
   CK_LAUNCH();
   d2h(hc.data(), cnt.p, nh);
   sync();
+  if (labels_out) *labels_out = std::move(lab);  // label = root position of the component
   return hc;
 }
 
@@ -3003,6 +3005,14 @@ void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_
   for (int g = 0; g < ngroups; g++) hstart[g] = gl.gn[g] ? gl.gstart[g] : 0;  // any valid row
   std::vector<int> c = count_components_level(gl.lv, gl.grp.p, N, hstart);
   for (int g = 0; g < ngroups; g++) counts[g] = gl.gn[g] ? c[g] : 0;
+}
+
+void part_component_labels(const long long *d_vtx, ll N, int nv, const int *d_part, int nparts,
+                           GroupLevel &gl, DBuf<int> &labels) {
+  build_group_level(d_vtx, N, nv, d_part, nparts, gl);
+  std::vector<ll> hstart(nparts, 0);
+  for (int g = 0; g < nparts; g++) hstart[g] = gl.gn[g] ? gl.gstart[g] : 0;
+  count_components_level(gl.lv, gl.grp.p, N, hstart, &labels);
 }
 
 void dual_graph_device(const long long *d_vtx, ll N, int nv, std::vector<ll> &rowptr,

@@ -106,6 +106,19 @@ struct GroupLevel {
 void build_group_level(const long long *d_vtx, ll N, int nv, const int *d_group_of,
                        int ngroups, GroupLevel &out);
 
+// Components of every part (part[e] in [0, nparts)): the part-ordered
+// level graph in gl and, per position of gl.perm, the label of its
+// component (the smallest position of the component).
+void part_component_labels(const long long *d_vtx, ll N, int nv, const int *d_part, int nparts,
+                           GroupLevel &gl, DBuf<int> &labels);
+
+// options.repair = 1: every part keeps its largest component; each other
+// component moves to the neighbouring part it shares the most dual-graph
+// weight with (ties: smallest part); isolated components stay.  d_part is
+// updated in place.
+void repair_parts_device(const long long *d_vtx, ll N, int nv, int nparts, int *d_part,
+                         long long *moved_components, long long *moved_elements);
+
 // Vertex-connected components of each group (group_of[e] < 0: no group);
 // counts (host, ngroups) receives the number per group.
 void components_device(const long long *d_vtx, ll N, int nv, const int *d_group_of,
