@@ -400,11 +400,11 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     atomicMax(any_active + 1, s.iters);  // active stays set until FIN_RESID_GATE
   } else if (OP == FIN_RESID_GATE) {
     // restart while the residual is above tol, at most mpass restarts, and
-    // stop after three restarts in a row within 10 tol that did not lower it
+    // stop after three restarts in a row within 2 tol that did not lower it
     // by 10% (the vector has reached what the working precision allows;
     // farther from tol a slow group keeps restarting)
     s.resid = __ddiv_rn(__dsqrt_rn(tot[0]), __dsqrt_rn(s.ff));
-    if (s.resid < 10.0 * tol && s.resid > 0.9 * s.prev_resid) s.stall += 1; else s.stall = 0;
+    if (s.resid < 2.0 * tol && s.resid > 0.9 * s.prev_resid) s.stall += 1; else s.stall = 0;
     s.prev_resid = s.resid;
     s.active = (!(s.resid <= tol) && s.npass < mpass && s.stall < 3) ? 1 : 0;
     if (s.active) atomicOr(any_active, 1);
