@@ -680,6 +680,9 @@ def main():
                                           [sum(st.lanczos_ms[i] for st in stats)
                                            for i in range(6)]])),
         "lanczos_spmv_ms": round(spmv_ms / len(stats), 2),
+        "lanczos_host_ms": dict(zip(["start_vectors", "graph_capture", "restart_loop",
+                                     "residual_check"],
+                                    [round(x, 2) for x in timed[-1].lanczos_host_ms])),
         "lanczos_passes": int(s.lanczos_passes),
     }
     if rank == 0:

@@ -174,6 +174,10 @@ typedef struct {
   long long level_steps[16];  /* Lanczos steps per bisection level (last: 15+) */
   long long repair_components;/* repair = 1: components moved to another part */
   long long repair_elements;  /*   and their elements */
+  double lanczos_host_ms[4];  /* host clock: start vectors (prediction +
+                                 judge), pass graph capture + instantiation,
+                                 the restart loop, the FP64 residual check +
+                                 download of each level */
 } parrsb_stats;
 
 enum {

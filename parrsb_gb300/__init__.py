@@ -65,13 +65,14 @@ class Stats(ctypes.Structure):
                 ("start_resid_warm", ctypes.c_double),
                 ("level_steps", ctypes.c_longlong * 16),
                 ("repair_components", ctypes.c_longlong),
-                ("repair_elements", ctypes.c_longlong)]
+                ("repair_elements", ctypes.c_longlong),
+                ("lanczos_host_ms", ctypes.c_double * 4)]
 
     def as_dict(self):
         d = {}
         for name, _ in self._fields_:
             v = getattr(self, name)
-            d[name] = list(v) if name in ("stage_ms", "lanczos_ms", "level_steps") else v
+            d[name] = list(v) if name in ("stage_ms", "lanczos_ms", "level_steps", "lanczos_host_ms") else v
         return d
 
 

@@ -23,6 +23,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <chrono>
 #include <array>
 
 #include "rsb.cuh"
@@ -1947,12 +1948,15 @@ struct Lanczos {
       for (auto &e : evk) CK(cudaEventCreate(&e));
     }
     if (use_graph) {
+      const auto h0 = std::chrono::steady_clock::now();
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       long long kl = ctx().kernel_launches;
       pass_body(lv, tol, mpass, &launches);
       ctx().kernel_launches = kl;
       CK(cudaStreamEndCapture(st, &graph));
       CK(cudaGraphInstantiate(&exec, graph, 0));
+      ctx().stats.lanczos_host_ms[1] +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
     }
     const long long per_pass_kernels =
         4 + (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) + 5 +
@@ -1962,6 +1966,7 @@ struct Lanczos {
     const bool level_log = !ev.empty() && getenv("PARRSB_GPU_LEVEL_LOG");
     const double spmv0 = ctx().stats.spmv_ms, pass0 = ctx().stats.lanczos_ms[5];
     int npass = 0;
+    const auto hp0 = std::chrono::steady_clock::now();
     for (int pass = 0; pass < mpass; pass++) {
       CK(cudaMemsetAsync(any.p, 0, 2 * sizeof(int), st));
       if (use_graph) {
@@ -1997,6 +2002,8 @@ struct Lanczos {
       }
       if (!h_any[0]) break;
     }
+    ctx().stats.lanczos_host_ms[2] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - hp0).count();
     if (level_log)
       fprintf(stderr,
               "parrsb_gb300: level rows=%lld groups=%d tiles=%d passes=%d steps=%lld "
@@ -2414,13 +2421,19 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
   lz.cg_factor = o.cg_factor;
   {
     StageTimer tm(PARRSB_STAGE_LANCZOS);
+    const auto h0 = std::chrono::steady_clock::now();
     if (y_warm) lz.choose_start(lv, y_warm, o.start, degen);
+    ctx().stats.lanczos_host_ms[0] +=
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
     lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, y_warm != nullptr, o.start);
   }
+  const auto h1 = std::chrono::steady_clock::now();
   if (o.check_resid) lz.residual(lv);
   k_to_double<VT><<<grid_for(N, 256), 256, 0, ctx().stream>>>(lz.f.p, N, f_pos);
   CK_LAUNCH();
   lz.download(res);
+  ctx().stats.lanczos_host_ms[3] +=
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h1).count();
 }
 
 }  // namespace
