@@ -1562,6 +1562,24 @@ __global__ void k_set_warm(GState *__restrict__ gs, int ngroups, const int *__re
   if (g < ngroups) gs[g].warm = use[g];
 }
 
+// Restarts driven on the device (a conditional while node of the pass
+// graph): the body zeroes the pass flags, runs one restart of every active
+// group and then k_loop_next folds the pass into the counters and sets the
+// condition: another restart only while a group is still active and fewer
+// than mpass restarts have run (so the loop always ends).
+__global__ void k_loop_zero(int *__restrict__ any) {
+  any[0] = 0;
+  any[1] = 0;
+}
+
+__global__ void k_loop_next(cudaGraphConditionalHandle h, const int *__restrict__ any,
+                            long long *__restrict__ ctr, int mpass) {
+  const long long np = ctr[0] + 1;
+  ctr[0] = np;
+  ctr[1] += any[1];  // steps of the longest group this restart
+  cudaGraphSetConditional(h, (any[0] != 0 && np < mpass) ? 1u : 0u);
+}
+
 // ----------------------------------------------------------------------------
 // Host-side segmented Lanczos engine
 // ----------------------------------------------------------------------------
@@ -1594,6 +1612,7 @@ struct Lanczos {
   // the same choice for the SpMV (PARRSB_GPU_SPMV_FUSED=1: fused)
   bool sp_fused = false;
   int ritz_bd = 256;             // threads per block of k_ritz
+  DBuf<long long> loop_ctr;      // device restart loop: passes, SpMV steps
   bool reorth = false;           // reorthogonalise every residual (opt-in)
   DBuf<double> part2, hro;       //   its tile partials and coefficients
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
@@ -1947,6 +1966,79 @@ struct Lanczos {
       evk.assign(4 * MI + 6, nullptr);
       for (auto &e : evk) CK(cudaEventCreate(&e));
     }
+    // the whole restart loop as one graph launch (no host round trip per
+    // restart), unless per-launch timing is on (no event nodes in a
+    // conditional body) or PARRSB_GPU_DEVICE_LOOP=0
+    static const bool device_loop_env = [] {
+      const char *e = getenv("PARRSB_GPU_DEVICE_LOOP");
+      return !(e && atoi(e) == 0);
+    }();
+    static bool device_loop_broken = false;
+    if (use_graph && ev.empty() && device_loop_env && !device_loop_broken) try {
+      const auto h0 = std::chrono::steady_clock::now();
+      CK(cudaGraphCreate(&graph, 0));
+      cudaGraphConditionalHandle hnd;
+      CK(cudaGraphConditionalHandleCreate(&hnd, graph, 1, cudaGraphCondAssignDefault));
+      cudaGraphNodeParams cp = {};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = hnd;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      loop_ctr.ensure(2);
+      CK(cudaMemsetAsync(loop_ctr.p, 0, 2 * sizeof(long long), st));
+      CK(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                       cudaStreamCaptureModeThreadLocal));
+      long long kl = ctx().kernel_launches;
+      k_loop_zero<<<1, 1, 0, st>>>(any.p);
+      pass_body(lv, tol, mpass, &launches);
+      k_loop_next<<<1, 1, 0, st>>>(hnd, any.p, loop_ctr.p, mpass);
+      ctx().kernel_launches = kl;
+      CK(cudaStreamEndCapture(st, &body));
+      CK(cudaGraphInstantiate(&exec, graph, 0));
+      ctx().stats.lanczos_host_ms[1] +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0)
+              .count();
+    } catch (const CudaError &e) {
+      // the graph could not be built or instantiated here: end any capture,
+      // report once, and run the restarts from the host from now on
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2 = nullptr;
+        cudaStreamEndCapture(st, &g2);
+        if (g2) cudaGraphDestroy(g2);
+      }
+      cudaGetLastError();
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      exec = nullptr, graph = nullptr;
+      device_loop_broken = true;
+      fprintf(stderr, "parrsb_gb300: device restart loop unavailable (%s); host loop used\n",
+              cudaGetErrorString(e.err));
+    }
+    if (exec) {  // the device loop was built
+      const auto h1 = std::chrono::steady_clock::now();
+      CK(cudaGraphLaunch(exec, st));
+      long long hc[2] = {0, 0};
+      d2h(hc, loop_ctr.p, 2);
+      sync();
+      const long long per_pass_kernels =
+          6 + (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) + 5 +
+          (resid_stop ? 4 : 0) + (reorth ? 3ll * MI : 0);
+      ctx().kernel_launches += per_pass_kernels * hc[0];
+      ctx().stats.lanczos_passes += hc[0];
+      ctx().stats.spmv_launches += hc[1];
+      ctx().stats.lanczos_host_ms[2] +=
+          std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h1)
+              .count();
+      cudaGraphExecDestroy(exec);
+      cudaGraphDestroy(graph);
+      exec = nullptr, graph = nullptr;
+      finish_run();
+      return;
+    }
     if (use_graph) {
       const auto h0 = std::chrono::steady_clock::now();
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -2018,14 +2110,19 @@ struct Lanczos {
     ctx().stats.spmv_launches += launches;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
+    finish_run();
+  }
+
+  // after the restarts: the staged SpMV's error flag, then normalise
+  // (src/fiedler.c:606-613) and fix the sign canonically: sum_i s_i f_i >= 0
+  // with s = +1 on the first half of the group's order
+  void finish_run() {
     {
       int h_err = 0;
       d2h(&h_err, err.p, 1);
       sync();
       if (h_err) throw CudaError{cudaErrorLaunchTimeout, __FILE__, __LINE__};  // a stage wait gave up
     }
-    // normalise (src/fiedler.c:606-613), then fix the sign canonically:
-    // sum_i s_i f_i >= 0 with s = +1 on the first half of the group's order
     tile<TM_SQ_F, GATE_ALL>();
     fin<FIN_NORM, GATE_ALL>();
     tile<TM_ORIENT, GATE_ALL>();
@@ -2428,7 +2525,10 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
     lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, y_warm != nullptr, o.start);
   }
   const auto h1 = std::chrono::steady_clock::now();
-  if (o.check_resid) lz.residual(lv);
+  // the residual-stop rule has already computed every group's FP64
+  // eigen-residual at its last restart (normalising and orienting the
+  // vector afterwards does not change it)
+  if (o.check_resid && !o.resid_stop) lz.residual(lv);
   k_to_double<VT><<<grid_for(N, 256), 256, 0, ctx().stream>>>(lz.f.p, N, f_pos);
   CK_LAUNCH();
   lz.download(res);
@@ -2517,6 +2617,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
   DBuf<int> perm((size_t)N), inv((size_t)N), grp((size_t)N), half((size_t)N),
       segpos((size_t)N), idx((size_t)N), moved((size_t)N), flag((size_t)N);
   DBuf<double> f_pos((size_t)N), f_tmp((size_t)N), y_pred;
+  DBuf<float4> esp;  // element spacings (warm starts only)
   DBuf<u64> keys((size_t)N);
   DBuf<int> vals((size_t)N), perm2((size_t)N);
   std::vector<HGroup> groups;
@@ -2606,11 +2707,16 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
         CK(cudaEventCreate(&w1));
         CK(cudaEventRecord(w0, st));
         y_pred.ensure((size_t)N);
+        if (!esp.p) {  // once per call: element spacings from the dual graph
+          esp.ensure((size_t)N);
+          element_spacings(G, cent, N, ndim, esp.p);
+        }
         if (use_net)
-          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p, &degen);
+          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p, &degen,
+                             esp.p);
         else  // start 2: the geometric guess
           geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p,
-                                  &degen);
+                                  &degen, esp.p);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;

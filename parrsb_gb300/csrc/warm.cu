@@ -168,6 +168,44 @@ k_mp_spacing(const FTile *__restrict__ tiles, const int *__restrict__ perm,
   }
 }
 
+// The same sums from per-element values (esp[e] = the element's own sums
+// over all its face neighbours, computed once per call from the dual graph):
+// a coalesced pass per level instead of the neighbour gathers.
+__global__ void __launch_bounds__(256)
+k_mp_spacing_elem(const FTile *__restrict__ tiles, const int *__restrict__ perm,
+                  const float4 *__restrict__ esp, double *__restrict__ part) {
+  const FTile t = tiles[blockIdx.x];
+  double s[4] = {0, 0, 0, 0};
+  for (ll i = t.b + threadIdx.x; i < t.e; i += blockDim.x) {
+    const float4 v = esp[perm[i]];
+    s[0] += v.x, s[1] += v.y, s[2] += v.z, s[3] += v.w;
+  }
+  __shared__ double sh[32];
+  for (int q = 0; q < 4; q++) {
+    const double v = mp_block_sum(s[q], sh);
+    if (threadIdx.x == 0) part[(ll)blockIdx.x * 4 + q] = v;
+    __syncthreads();
+  }
+}
+
+__global__ void k_elem_spacing(const ll *__restrict__ rowptr, const int *__restrict__ col,
+                               const unsigned char *__restrict__ w, const double *__restrict__ cent,
+                               ll nel, unsigned wface, float4 *__restrict__ esp) {
+  const ll e = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  double s[4] = {0, 0, 0, 0};
+  for (ll q = rowptr[e]; q < rowptr[e + 1]; q++) {
+    if (w[q] != wface) continue;
+    const int f = col[q];
+    for (int a = 0; a < 3; a++) {
+      const double d = cent[(ll)a * nel + e] - cent[(ll)a * nel + f];
+      s[a] += d * d;
+    }
+    s[3] += 1.0;
+  }
+  esp[e] = make_float4((float)s[0], (float)s[1], (float)s[2], (float)s[3]);
+}
+
 // sa[g][a] = 1 / h_a (1 where an axis has no spacing: 2D z, no pairs)
 __global__ void k_mp_scales(const double *__restrict__ part, const int *__restrict__ tile0,
                             const int *__restrict__ ntile, int ngroups,
@@ -953,15 +991,15 @@ inline unsigned mp_grid(ll Npad) {
 }
 
 void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame,
-               std::vector<int> *degen = nullptr);
+               std::vector<int> *degen = nullptr, const float4 *esp = nullptr);
 
 void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffers &B,
-                 std::vector<int> *degen = nullptr) {
+                 std::vector<int> *degen = nullptr, const float4 *esp = nullptr) {
   cudaStream_t st = ctx().stream;
   B.X.ensure((size_t)v.Npad * MP_FIN);
   B.wsum.ensure((size_t)v.Npad);
   DBuf<double> frame;
-  mp_frames(v, cent, nel, ndim, frame, degen);
+  mp_frames(v, cent, nel, ndim, frame, degen, esp);
   k_mp_features<<<grid_for(v.Npad, 256), 256, 0, st>>>(
       v.perm, v.grp, cent, nel, frame.p, v.lv->ell.p, v.lv->slice_off.p, v.lv->slice_w.p, v.N,
       v.Npad, B.X.p, B.wsum.p);
@@ -971,7 +1009,7 @@ void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffer
 // Per group: {mu[3], R[3][3], 1/s} (k_mp_frames); degen (optional): per
 // group, 1 when its two largest centroid variances are within 5%.
 void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame,
-               std::vector<int> *degen) {
+               std::vector<int> *degen, const float4 *esp) {
   cudaStream_t st = ctx().stream;
   const int G = (int)v.gstart.size();
   std::vector<FTile> tiles;
@@ -996,9 +1034,12 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     h2d(gn.p, v.gn.data(), G);
     DBuf<double> part(tiles.size() * 9);
     const unsigned wface = ndim == 3 ? 4u : 2u;  // face (3D) or edge (2D) neighbours
-    k_mp_spacing<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, v.perm, cent, nel, v.lv->ell.p,
-                                                        v.lv->slice_off.p, v.lv->slice_w.p,
-                                                        wface, part.p);
+    if (esp)
+      k_mp_spacing_elem<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, v.perm, esp, part.p);
+    else
+      k_mp_spacing<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, v.perm, cent, nel,
+                                                          v.lv->ell.p, v.lv->slice_off.p,
+                                                          v.lv->slice_w.p, wface, part.p);
     CK_LAUNCH();
     k_mp_scales<<<grid_for(G, 128), 128, 0, st>>>(part.p, d0.p, dn.p, G, sa.p);
     CK_LAUNCH();
@@ -1133,22 +1174,30 @@ bool warm_net_ready() {
   return g_net[dev].ready;
 }
 
+void element_spacings(const Graph &g, const double *cent, ll nel, int ndim, float4 *esp) {
+  if (nel <= 0) return;
+  k_elem_spacing<<<grid_for(nel, 256), 256, 0, ctx().stream>>>(
+      g.rowptr.p, g.col.p, g.w.p, cent, nel, ndim == 3 ? 4u : 2u, esp);
+  CK_LAUNCH();
+}
+
 void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
                              const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
                              const std::vector<ll> &gn, ll N, double *y,
-                             std::vector<int> *degen) {
+                             std::vector<int> *degen, const float4 *esp) {
   MpView v;
   v.lv = &lv, v.perm = perm, v.grp = grp, v.N = N, v.Npad = (N + MP_ROWS - 1) / MP_ROWS * MP_ROWS;
   v.gstart = gstart, v.gn = gn;
   DBuf<double> frame;
-  mp_frames(v, cent, nel, ndim, frame, degen);
+  mp_frames(v, cent, nel, ndim, frame, degen, esp);
   k_mp_geometric<<<grid_for(N, 256), 256, 0, ctx().stream>>>(perm, grp, cent, nel, frame.p, N, y);
   CK_LAUNCH();
 }
 
 void warm_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
                         ll nel, int ndim, const std::vector<ll> &gstart,
-                        const std::vector<ll> &gn, ll N, double *y, std::vector<int> *degen) {
+                        const std::vector<ll> &gn, ll N, double *y, std::vector<int> *degen,
+                        const float4 *esp) {
   int dev = 0;
   CK(cudaGetDevice(&dev));
   NetDev net;
@@ -1163,7 +1212,7 @@ void warm_predict_level(const Level &lv, const int *perm, const int *grp, const 
   v.lv = &lv, v.perm = perm, v.grp = grp, v.N = N, v.Npad = (N + MP_ROWS - 1) / MP_ROWS * MP_ROWS;
   v.gstart = gstart, v.gn = gn;
   MpBuffers B;
-  mp_features(v, cent, nel, ndim, B, degen);
+  mp_features(v, cent, nel, ndim, B, degen, esp);
   mp_forward(v, net, B, false);
   k_mp_y_to_double<<<grid_for(N, 256), 256, 0, ctx().stream>>>(B.y.p, grp, N, y);
   CK_LAUNCH();

@@ -47,13 +47,19 @@ bool warm_net_ready();
 void warm_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
                         ll nel, int ndim, const std::vector<ll> &gstart,
                         const std::vector<ll> &gn, ll N, double *y,
-                        std::vector<int> *degen = nullptr);
+                        std::vector<int> *degen = nullptr, const float4 *esp = nullptr);
 
 // The geometric start of the same groups: -sin(pi x~_1 / 2) along each
 // group's principal axis (x~_1 as in the network's first input feature).
 void geometric_predict_level(const Level &lv, const int *perm, const int *grp,
                              const double *cent, ll nel, int ndim, const std::vector<ll> &gstart,
                              const std::vector<ll> &gn, ll N, double *y,
-                             std::vector<int> *degen = nullptr);
+                             std::vector<int> *degen = nullptr, const float4 *esp = nullptr);
+
+// Per element, over its face neighbours in the dual graph g (weight 4 in 3D,
+// 2 in 2D): the sums of the squared centroid differences per axis and the
+// neighbour count (the element-spacing input of the frames; esp may then be
+// passed to the predictions above instead of their per-level pass).
+void element_spacings(const Graph &g, const double *cent, ll nel, int ndim, float4 *esp);
 
 }  // namespace prsb

@@ -373,3 +373,22 @@ def test_rsb_fused_finalisation_same_bits(monkeypatch, fp32):
     monkeypatch.setenv("PARRSB_GPU_SPMV_FUSED", "1")
     b = P.part_mesh(vtx, xyz, 8, partitioner=0)
     np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("stop", ["0", "1"])
+def test_device_restart_loop_same_bits(monkeypatch, stop):
+    """The restarts run inside one graph launch (a conditional while node
+    that the last kernel of each restart sets) or from the host, one graph
+    launch per restart: bitwise the same partition and step counts."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", "1")
+    monkeypatch.setenv("PARRSB_GPU_RESID_STOP", stop)
+    vtx, xyz = meshgen.box_hex(24, 20, 12, jitter=0.1, seed=17)
+    a = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    sa = P.last_stats()
+    monkeypatch.setenv("PARRSB_GPU_DEVICE_LOOP", "0")
+    b = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    sb = P.last_stats()
+    np.testing.assert_array_equal(a, b)
+    assert sa.lanczos_iters == sb.lanczos_iters
+    assert sa.lanczos_passes == sb.lanczos_passes
+    assert sa.spmv_launches == sb.spmv_launches
