@@ -1969,7 +1969,7 @@ struct Lanczos {
     // the whole restart loop as one graph launch (no host round trip per
     // restart), unless per-launch timing is on (no event nodes in a
     // conditional body) or PARRSB_GPU_DEVICE_LOOP=0
-    static const bool device_loop_env = [] {
+    const bool device_loop_env = [] {
       const char *e = getenv("PARRSB_GPU_DEVICE_LOOP");
       return !(e && atoi(e) == 0);
     }();
