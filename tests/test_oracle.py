@@ -340,3 +340,20 @@ def test_dual_graph_weights_are_run_occurrences(oracle, seed):
         got = dict(rows[a])
         assert got == want, a
         assert len(rows[a]) == len(got)  # each neighbour listed once
+
+
+def test_oracle_threads_do_not_change_results(oracle):
+    """The oracle splits sums into fixed blocks of 65,536 values and runs
+    the halves of a bisection on disjoint scratch: 1 or 4 host threads give
+    bitwise the same partition, Lanczos steps and residual."""
+    from parrsb_gb300 import meshgen
+    vtx, xyz = meshgen.box_hex(48, 40, 40, jitter=0.1, seed=3)  # 76,800 > one block
+    res = []
+    for t in (1, 4):
+        oracle.threads(t)
+        rc, part, _, info, _ = oracle.part_mesh(vtx, xyz, 16, partitioner=0)
+        assert rc == 0
+        res.append((part, info.total_iters, info.max_resid))
+    oracle.threads(0)
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    assert res[0][1] == res[1][1] and res[0][2] == res[1][2]
