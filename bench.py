@@ -51,9 +51,10 @@ def parse():
     ap.add_argument("--shape", default=None, help="override mesh shape nx,ny,nz")
     ap.add_argument("--nparts", type=int, default=None)
     ap.add_argument("--fp32", type=int, default=None)
-    ap.add_argument("--method", default="warm", choices=["warm", "reference"],
+    ap.add_argument("--method", default="warm", choices=["warm", "reference", "learned"],
                     help="warm: geometric warm start + residual stop; reference: the "
-                         "reference's start vector and stopping rule")
+                         "reference's start vector and stopping rule; learned: the "
+                         "learned warm start (network) + residual stop")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-plain", action="store_true",
@@ -373,9 +374,10 @@ def main():
     # the reference's start vector and stopping rule)
     os.environ["PARRSB_GPU_FP32"] = str(1 if args.fp32 is None else args.fp32)
     method_env = ({"PARRSB_GPU_START": "2", "PARRSB_GPU_RESID_STOP": "1"}
-                  if args.method == "warm" else
+                  if args.method in ("warm", "learned") else
                   {"PARRSB_GPU_START": "0", "PARRSB_GPU_RESID_STOP": "0"})
-    method_env.update({"PARRSB_GPU_WARM": "0", "PARRSB_GPU_WARM_MIN": "0"})
+    method_env.update({"PARRSB_GPU_WARM": "1" if args.method == "learned" else "0",
+                       "PARRSB_GPU_WARM_MIN": "0"})
     os.environ.update(method_env)
     os.environ.setdefault("PARRSB_VERBOSE_LEVEL", "0")
     import parrsb_gb300 as P
@@ -637,9 +639,11 @@ def main():
                              "axis in element spacings, judged per group against the "
                              "reference's step start by FP64 eigen-residual; groups with two "
                              "axes within 5% keep the step start"
-                             if args.method == "warm" else "the reference's step start"),
+                             if args.method == "warm" else
+                             "learned warm start (network), judged per group the same way"
+                             if args.method == "learned" else "the reference's step start"),
                    "stop": ("restart until the FP64 eigen-residual <= rsb_tol"
-                            if args.method == "warm" else
+                            if args.method in ("warm", "learned") else
                             "the reference's CG-residual rule"),
                    "learned_start": "see start_vectors.learned_* (network inference cost "
                                     "included)",
