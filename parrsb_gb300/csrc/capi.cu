@@ -7,6 +7,7 @@
 // the caller's struct, levels clamped to 2, rsb_pre = 0 without coordinates)
 // follows src/parrsb.c:26-77, 229, 250.  Errors are returned, never exit().
 #include <stdarg.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -179,6 +180,58 @@ int prepare_options(const long long *vtx, const double *xyz, int nel, int nv,
     if (vtx == nullptr) return PARRSB_ERR_ARGS;
   }
   return PARRSB_OK;
+}
+
+// Host inputs into device buffers.  When the host buffer is page-locked and
+// mapped into the device's address space (cudaHostAlloc / cudaHostRegister
+// memory under unified addressing), the GPU's SMs read it directly over the
+// host link with 16-byte loads; otherwise a cudaMemcpyAsync stages it.
+// (Copy-engine transfers of the same 2 GB ran between 211 and 25 GB/s
+// depending on the call's stream and on device memory state; SM reads do
+// not depend on either.)  PARRSB_GPU_UPLOAD=copy forces the copy engine.
+__global__ void k_pull_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst, ll n16) {
+  for (ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x; i < n16;
+       i += (ll)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+__global__ void k_pull_host_tail(const unsigned char *__restrict__ src,
+                                 unsigned char *__restrict__ dst, ll n) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
+template <typename T>
+void upload(T *d, const T *h, size_t n) {
+  if (!n) return;
+  static const bool force_copy = [] {
+    const char *e = getenv("PARRSB_GPU_UPLOAD");
+    return e && strcmp(e, "copy") == 0;
+  }();
+  cudaPointerAttributes a;
+  const size_t bytes = n * sizeof(T);
+  if (!force_copy && cudaPointerGetAttributes(&a, h) == cudaSuccess &&
+      a.type == cudaMemoryTypeHost && a.devicePointer != nullptr &&
+      reinterpret_cast<uintptr_t>(a.devicePointer) % 16 == 0 &&
+      reinterpret_cast<uintptr_t>(d) % 16 == 0) {
+    const ll n16 = (ll)(bytes / 16);
+    const unsigned grid = (unsigned)std::min<ll>(std::max<ll>(1, (n16 + 255) / 256), 152 * 16);
+    if (n16 > 0) {
+      k_pull_host<<<grid, 256, 0, ctx().stream>>>(static_cast<const uint4 *>(a.devicePointer),
+                                                  reinterpret_cast<uint4 *>(d), n16);
+      CK_LAUNCH();
+    }
+    const ll tail = (ll)(bytes - (size_t)n16 * 16);
+    if (tail > 0) {
+      k_pull_host_tail<<<1, 256, 0, ctx().stream>>>(
+          static_cast<const unsigned char *>(a.devicePointer) + n16 * 16,
+          reinterpret_cast<unsigned char *>(d) + n16 * 16, tail);
+      CK_LAUNCH();
+    }
+    return;
+  }
+  cudaGetLastError();  // a pageable pointer is not an error
+  h2d(d, h, n);
 }
 
 // PARRSB_GPU_WARM_WEIGHTS=<file>: the warm-start network's parameters as
@@ -460,11 +513,11 @@ static int part_mesh_host(int *part, int *seq, const long long *vtx, const doubl
       StageTimer tm(PARRSB_STAGE_UPLOAD);
       if (vtx) {
         W.vtx.ensure((size_t)N * nv);
-        h2d(W.vtx.p, vtx, (size_t)N * nv);
+        upload(W.vtx.p, vtx, (size_t)N * nv);
       }
       if (xyz) {
         W.xyz.ensure((size_t)N * nv * ndim);
-        h2d(W.xyz.p, xyz, (size_t)N * nv * ndim);
+        upload(W.xyz.p, xyz, (size_t)N * nv * ndim);
       }
       W.part.ensure((size_t)N);
     }
@@ -529,7 +582,7 @@ extern "C" int parrsb_conn_mesh(long long *vtx, double *coord, unsigned int nel,
     {
       StageTimer tm(PARRSB_STAGE_UPLOAD);
       W.xyz.ensure((size_t)np * nDim);
-      h2d(W.xyz.p, coord, (size_t)np * nDim);
+      upload(W.xyz.p, coord, (size_t)np * nDim);
       W.ids.ensure((size_t)np);
     }
     ll nseg = 0;
