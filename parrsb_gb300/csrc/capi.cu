@@ -186,9 +186,10 @@ int prepare_options(const long long *vtx, const double *xyz, int nel, int nv,
 // mapped into the device's address space (cudaHostAlloc / cudaHostRegister
 // memory under unified addressing), the GPU's SMs read it directly over the
 // host link with 16-byte loads; otherwise a cudaMemcpyAsync stages it.
-// (Copy-engine transfers of the same 2 GB ran between 211 and 25 GB/s
-// depending on the call's stream and on device memory state; SM reads do
-// not depend on either.)  PARRSB_GPU_UPLOAD=copy forces the copy engine.
+// (Measured on a GB300 with 2.15 GB of pinned inputs: SM reads 10.2 ms on
+// every call, the link's 211 GB/s; copy-engine transfers of the same
+// buffers 10-21 ms, slower after RSB calls, and 25-90 ms in some
+// processes.)  PARRSB_GPU_UPLOAD=copy forces the copy engine.
 __global__ void k_pull_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst, ll n16) {
   for (ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x; i < n16;
        i += (ll)gridDim.x * blockDim.x)
