@@ -313,12 +313,24 @@ enum FinOp {
   FIN_RESID_GATE   // residual of the Ritz vector; restart while above tol
 };
 
-// One block per group: reduce the group's tile partials in a fixed order and
-// apply the scalar update of the Lanczos recurrence.
-// Reduce group g's tile partials in a fixed order (thread-strided sequential
-// sums, then the block tree) and apply the scalar update OP.  Run by a whole
-// block: either the dedicated k_fin launch or, fused, the last tile block of
-// the group to finish.
+// The scalar update OP of group g from its reduced tile partials tot, by
+// one thread.  owner = false leaves the per-group arrays (diagT, upperT,
+// vnorm) untouched: the persistent step kernel applies the step updates in
+// every block that holds a tile of the group (same inputs, same result) and
+// lets one block write them.
+template <int OP>
+__device__ __forceinline__ void fin_apply(GState &s, int g, double tot0, double tot1, int it,
+                                          int MI, double tol, int mpass,
+                                          double *__restrict__ diagT,
+                                          double *__restrict__ upperT,
+                                          double *__restrict__ vnorm,
+                                          int *__restrict__ any_active, bool owner);
+
+// One block per group: reduce the group's tile partials in a fixed order
+// (thread-strided sequential sums, then the block tree of LZ_THREADS
+// threads) and apply the scalar update OP.  Run by a whole block: either the
+// dedicated k_fin launch or, fused, the last tile block of the group to
+// finish.
 template <int OP>
 __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int it, int MI,
                          double tol, int mpass, double *__restrict__ diagT,
@@ -344,6 +356,18 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     }
   }
   if (threadIdx.x != 0) return;
+  fin_apply<OP>(s, g, tot[0], tot[1], it, MI, tol, mpass, diagT, upperT, vnorm, any_active,
+                true);
+}
+
+template <int OP>
+__device__ __forceinline__ void fin_apply(GState &s, int g, double tot0, double tot1, int it,
+                                          int MI, double tol, int mpass,
+                                          double *__restrict__ diagT,
+                                          double *__restrict__ upperT,
+                                          double *__restrict__ vnorm,
+                                          int *__restrict__ any_active, bool owner) {
+  const double tot[2] = {tot0, tot1};
   double dn = (double)s.n;
   if (OP == FIN_IV_MEAN || OP == FIN_INIT_MEAN || OP == FIN_PMEAN || OP == FIN_RITZ_MEAN) {
     s.c = __ddiv_rn(tot[0], dn);
@@ -354,7 +378,7 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     double rnorm = __dsqrt_rn(rtr);
     s.rnorm = rnorm;
     s.rtol = __dmul_rn(rnorm, tol);
-    vnorm[(ll)g * (MI + 1)] = rnorm;
+    if (owner) vnorm[(ll)g * (MI + 1)] = rnorm;
     s.rtz2 = 1.0;
     s.rtz1 = rtr;
     s.beta = 0.0;
@@ -366,7 +390,8 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     double pap = tot[0], pap_old = s.pap;
     s.pap = pap;
     s.alpha = __ddiv_rn(s.rtz1, pap);
-    if (it == 0) {
+    if (!owner) {
+    } else if (it == 0) {
       diagT[(ll)g * MI] = __ddiv_rn(pap, s.rtz1);
     } else {
       double bb = __dmul_rn(s.beta, s.beta);
@@ -377,7 +402,7 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
   } else if (OP == FIN_RTR) {
     double rtr = tot[0];
     double rnorm = __dsqrt_rn(rtr);
-    vnorm[(ll)g * (MI + 1) + it + 1] = rnorm;
+    if (owner) vnorm[(ll)g * (MI + 1) + it + 1] = rnorm;
     s.rnorm = rnorm;
     s.iters = it + 1;
     if (rnorm < s.rtol) {
@@ -671,6 +696,153 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   }
 }
 
+// ---------------------------------------------------------------------------
+// y = L f of the residual check for FP32 vectors, exact in 64-bit fixed
+// point on the integer pipe instead of one FP64 subtract, multiply and add
+// (plus two conversions) per nonzero on the FP64 pipe, which runs at 1/64 of
+// the FP32 rate.  Each group's f is scaled by 2^S_g so that its largest
+// |f| lies in [2^46, 2^47) and truncated to integers Fq (entries at least
+// 2^-22 of the group's largest are exact; smaller ones lose at most
+// 2^-47 of it).  Then y_i = d_i Fq_i - sum_j w_ij Fq_j is exact in int64
+// for rows of fewer than 2048 stored entries (|terms| < 2^51 each) and is
+// rounded once to FP64.  The sums f.y and f.f and their reduction order are
+// those of the FP64 form (TM_RESID1 of k_tile).
+// ---------------------------------------------------------------------------
+constexpr int RQ_MAX_WIDTH = 2048;  // widest ELL slice the integer form accepts
+
+// per tile: the largest |f| of the tile's rows (IEEE bits, which order like
+// the magnitudes)
+template <int GATE>
+__global__ void __launch_bounds__(512)
+k_rq_max(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+         const GState *__restrict__ gs, const float *__restrict__ f, unsigned *__restrict__ tmax) {
+  pdl_entry();
+  __shared__ unsigned wm[16];
+  const int t = blockIdx.x, g = tgrp[t];
+  if (!gate_ok(gs[g], GATE)) return;
+  unsigned m = 0;
+  for (ll i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x)
+    m = max(m, __float_as_uint(f[i]) & 0x7FFFFFFFu);
+  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(blockDim.x >> 5); k++) m = max(m, wm[k]);
+    tmax[t] = m;
+  }
+}
+
+// the group's largest |f| from its tiles' maxima (every block of the group
+// computes it; the block of the group's first tile also stores it)
+__device__ __forceinline__ unsigned rq_group_max(const GState &s, int t,
+                                                 const unsigned *__restrict__ tmax,
+                                                 unsigned *__restrict__ gmax, int g) {
+  __shared__ unsigned wm[16];
+  unsigned m = 0;
+  for (int q = threadIdx.x; q < s.ntiles; q += blockDim.x) m = max(m, tmax[s.tile0 + q]);
+  for (int off = 16; off > 0; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = wm[0];
+  for (int k = 1; k < (int)(blockDim.x >> 5); k++) m = max(m, wm[k]);
+  if (threadIdx.x == 0 && t == s.tile0) gmax[g] = m;
+  return m;
+}
+
+// S_g - 150 + 23 folded: an entry of biased exponent E is shifted by
+// E - Emax + 23 (Emax: biased exponent of the group's largest |f|)
+__device__ __forceinline__ ll rq_quantize(float x, unsigned gm) {
+  const unsigned u = __float_as_uint(x);
+  const int E = (int)((u >> 23) & 0xFF);
+  if (E == 0) return 0;  // zero and subnormals (below 2^-126)
+  const ll m = (ll)((u & 0x7FFFFFu) | 0x800000u);
+  const int sh = E - (int)(gm >> 23) + 23;
+  const ll v = sh >= 0 ? (m << sh) : (sh > -24 ? (m >> -sh) : 0);
+  return (u >> 31) ? -v : v;
+}
+
+template <int GATE>
+__global__ void __launch_bounds__(512)
+k_rq_quant(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+           const GState *__restrict__ gs, const float *__restrict__ f,
+           const unsigned *__restrict__ tmax, unsigned *__restrict__ gmax,
+           ll *__restrict__ fq) {
+  pdl_entry();
+  const int t = blockIdx.x, g = tgrp[t];
+  if (!gate_ok(gs[g], GATE)) return;
+  const unsigned gm = rq_group_max(gs[g], t, tmax, gmax, g);
+  for (ll i = tbeg[t] + threadIdx.x; i < tend[t]; i += blockDim.x) fq[i] = rq_quantize(f[i], gm);
+}
+
+template <int GATE>
+__global__ void __launch_bounds__(512)
+k_rq_resid1(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
+            const int *__restrict__ tgrp, const GState *__restrict__ gs,
+            const float *__restrict__ f, const ll *__restrict__ fq,
+            const unsigned *__restrict__ gmax, const unsigned *__restrict__ ell,
+            const ll *__restrict__ slice_off, const int *__restrict__ slice_w,
+            double *__restrict__ y64, double *__restrict__ part) {
+  pdl_entry();
+  __shared__ double cs[2][LZ_TILE / 32 + 1];
+  const int t = blockIdx.x, g = tgrp[t];
+  if (!gate_ok(gs[g], GATE)) return;
+  const unsigned gm = gmax[g];
+  // 2^-S_g with S_g = 46 - (Emax - 127); a group whose largest |f| is not
+  // finite gets NaN (its residual then never wins and never passes)
+  const bool finite = gm < 0x7F800000u;
+  const double unscale =
+      __longlong_as_double((ll)(1023 - 46 + ((int)(gm >> 23) - 127)) << 52);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const ll b = tbeg[t], e = tend[t];
+  const ll c0 = b >> 5;
+  const int nc = (int)(((e - 1) >> 5) - c0 + 1);
+  for (int q = warp; q < nc; q += nw) {
+    const ll i = (c0 + q) * 32 + lane;
+    const bool valid = i >= b && i < e;
+    double d1 = 0.0, d2 = 0.0;
+    if (valid) {
+      const ll sl = i >> 5;
+      const unsigned *ep = ell + slice_off[sl] + (i & 31);
+      const int wd = slice_w[sl];
+      ll acc = 0;
+      int dsum = 0;
+      int k = 0;
+#pragma unroll 1
+      for (; k + 8 <= wd; k += 8) {
+        unsigned x[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) x[u] = __ldcs(ep + (ll)(k + u) * 32);
+        ll fj[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) fj[u] = fq[x[u] & 0x0FFFFFFFu];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          acc += (ll)(x[u] >> 28) * fj[u];
+          dsum += (int)(x[u] >> 28);
+        }
+      }
+      for (; k < wd; k++) {
+        const unsigned x = __ldcs(ep + (ll)k * 32);
+        acc += (ll)(x >> 28) * fq[x & 0x0FFFFFFFu];
+        dsum += (int)(x >> 28);
+      }
+      const ll yq = (ll)dsum * fq[i] - acc;
+      const double yv = finite ? __dmul_rn(__ll2double_rn(yq), unscale) : __longlong_as_double(0x7FF8000000000000ll);
+      y64[i] = yv;
+      const double fi = (double)f[i];
+      d1 = __dmul_rn(fi, yv);
+      d2 = __dmul_rn(fi, fi);
+    }
+    const double v1 = warp_tree_sum(d1), v2 = warp_tree_sum(d2);
+    if (lane == 0) cs[0][q] = v1, cs[1][q] = v2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const double v0 = tile_total(cs[0], nc), v1 = tile_total(cs[1], nc);
+    if (threadIdx.x == 0) part[2 * t] = v0, part[2 * t + 1] = v1;
+  }
+}
+
 // Rows per lane of the vectorised tile kernels: one 16-byte load per array.
 template <typename VT>
 struct VecOf;
@@ -751,28 +923,18 @@ __device__ __forceinline__ double LaneSum<double>::chunk() const { return warp_t
 // one chunk per warp on smaller ones so that enough warps fill the GPU
 constexpr ll PR_BIG = 1ll << 22;
 
-template <typename VT, int MODE, int PR_U, bool FUSE = true>
-__global__ void __launch_bounds__(512)
-k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
-     GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
-     VT *__restrict__ V, ll N, double *__restrict__ part, FinArgs fa) {
-  pdl_entry();
+// One tile [b, e) of a vector update: the rows, then (thread 0) the tile
+// partial into *out.  Called by every thread of the block.
+template <typename VT, int MODE, int PR_U>
+__device__ __forceinline__ void pr_tile(ll b, ll e, VT c, VT beta, VT alpha, int it,
+                                        VT *__restrict__ p, const VT *__restrict__ w,
+                                        VT *__restrict__ V, ll N, double *cs, float2 *cs2,
+                                        double *__restrict__ part, int t) {
   using Vec = VecOf<VT>;
   constexpr int R = Vec::R, CH = 32 * R;
-  constexpr int OP = MODE == TM_P ? FIN_PMEAN : FIN_RTR;
-  __shared__ double sh[32];
-  __shared__ double cs[LZ_TILE / CH + 2];
-  __shared__ float2 cs2[LZ_TILE / CH + 2];  // chunk pairs (FP32)
-  const int t = blockIdx.x;
-  const int g = tgrp[t];
-  const GState &s = gs[g];
-  if (!s.run) return;
-  const int it = fa.it;
-  const VT c = (VT)s.c, beta = (VT)s.beta, alpha = (VT)s.alpha;
   const VT *__restrict__ rv = V + (ll)it * N;
   VT *__restrict__ rn = V + (ll)(it + 1) * N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const ll b = tbeg[t], e = tend[t];
   const ll c0 = b / CH;
   const int nc = (int)((e - 1) / CH - c0 + 1);
   for (int q0 = PR_U * warp; q0 < nc; q0 += PR_U * nw) {
@@ -818,6 +980,25 @@ k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__rest
     const double v0 = sizeof(VT) == 4 ? tile_total_pair(cs2, nc) : tile_total(cs, nc);
     if (threadIdx.x == 0) part[t] = v0;
   }
+}
+
+template <typename VT, int MODE, int PR_U, bool FUSE = true>
+__global__ void __launch_bounds__(512)
+k_pr(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *__restrict__ tgrp,
+     GState *__restrict__ gs, VT *__restrict__ p, const VT *__restrict__ w,
+     VT *__restrict__ V, ll N, double *__restrict__ part, FinArgs fa) {
+  pdl_entry();
+  constexpr int CH = 32 * VecOf<VT>::R;
+  constexpr int OP = MODE == TM_P ? FIN_PMEAN : FIN_RTR;
+  __shared__ double sh[32];
+  __shared__ double cs[LZ_TILE / CH + 2];
+  __shared__ float2 cs2[LZ_TILE / CH + 2];  // chunk pairs (FP32)
+  const int t = blockIdx.x;
+  const int g = tgrp[t];
+  const GState &s = gs[g];
+  if (!s.run) return;
+  pr_tile<VT, MODE, PR_U>(tbeg[t], tend[t], (VT)s.c, (VT)s.beta, (VT)s.alpha, fa.it, p, w, V, N,
+                          cs, cs2, part, t);
   if (FUSE) fused_fin<OP>(gs, g, part, fa, sh);
 }
 
@@ -839,26 +1020,17 @@ inline int vec_threads(ll rows, int chunks_per_warp) {
 // loads, uniform width).  The index stream is read with the evict-first
 // policy so that the vectors (p, w, the Krylov rows) stay in L2 between the
 // launches of a step.
+// One tile [b, e) of the SpMV: w = L p on the tile's rows, then (thread 0)
+// the tile partial of sum w (p - c) into *out.  Called by every thread of
+// the block; wlut holds the weights 0..15 as doubles (FP64 form).
 template <typename VT>
-__global__ void __launch_bounds__(512)
-k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
-       const int *__restrict__ tgrp, GState *__restrict__ gs,
-       const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
-       const int *__restrict__ slice_w, const VT *__restrict__ p, VT *__restrict__ w,
-       double *__restrict__ part, FinArgs fa, int fuse, int force) {
-  pdl_entry();
-  __shared__ double sh[32];
-  __shared__ double cs[LZ_TILE / 32 + 1];
-  __shared__ float2 cs2[LZ_TILE / 32 + 1];  // chunk pairs (FP32)
-  __shared__ double wlut[16];
-  if (threadIdx.x < 16) wlut[threadIdx.x] = (double)threadIdx.x;
-  __syncthreads();
-  int t = blockIdx.x;
-  int g = tgrp[t];
-  if (!gs[g].run && !force) return;
-  const VT c = (VT)gs[g].c;
+__device__ __forceinline__ void spmv_tile(ll b, ll e, VT c, const unsigned *__restrict__ ell,
+                                          const ll *__restrict__ slice_off,
+                                          const int *__restrict__ slice_w,
+                                          const VT *__restrict__ p, VT *__restrict__ w,
+                                          const double *wlut, double *cs, float2 *cs2,
+                                          double *__restrict__ part, int t) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const ll b = tbeg[t], e = tend[t];
   const ll c0 = b >> 5;
   const int nc = (int)(((e - 1) >> 5) - c0 + 1);
   for (int q = warp; q < nc; q += nw) {
@@ -932,6 +1104,27 @@ k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     const double v0 = sizeof(VT) == 4 ? tile_total_pair(cs2, nc) : tile_total(cs, nc);
     if (threadIdx.x == 0) part[t] = v0;
   }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(512)
+k_spmv(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
+       const int *__restrict__ tgrp, GState *__restrict__ gs,
+       const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+       const int *__restrict__ slice_w, const VT *__restrict__ p, VT *__restrict__ w,
+       double *__restrict__ part, FinArgs fa, int fuse, int force) {
+  pdl_entry();
+  __shared__ double sh[32];
+  __shared__ double cs[LZ_TILE / 32 + 1];
+  __shared__ float2 cs2[LZ_TILE / 32 + 1];  // chunk pairs (FP32)
+  __shared__ double wlut[16];
+  if (threadIdx.x < 16) wlut[threadIdx.x] = (double)threadIdx.x;
+  __syncthreads();
+  int t = blockIdx.x;
+  int g = tgrp[t];
+  if (!gs[g].run && !force) return;
+  spmv_tile<VT>(tbeg[t], tend[t], (VT)gs[g].c, ell, slice_off, slice_w, p, w, wlut, cs, cs2,
+                part, t);
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
 }
 
@@ -1107,6 +1300,216 @@ k_spmv_tma(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
     }
   }
   if (fuse) fused_fin<FIN_PAP>(gs, g, part, fa, sh);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent segmented step kernel: every Lanczos step of a pass
+// (src/fiedler.c:458-504) for all groups of the level in one cooperative
+// launch, in place of the six launches per step (P update, its
+// finalisation, SpMV, finalisation, R update, finalisation).  Block b owns
+// tiles b, b + G, b + 2G, ... (G blocks, all resident: a cooperative launch
+// refuses a grid that does not fit).  A step is three phases separated by
+// grid barriers; each phase runs the same tile body as the stand-alone
+// kernel (pr_tile, spmv_tile) and writes the same tile partials, into a
+// partial array of its own.  After a barrier every block reduces, for each
+// of its tiles whose group runs, the group's partials in the order of k_fin
+// (256 virtual threads: strided sequential sums, warp trees, the warps in
+// order) and applies the scalar update to its own copy of the group state
+// in shared memory; the block holding the group's first tile writes the
+// per-group arrays and, at the end, the state.  Results are bitwise those of
+// the launch-per-kernel pass.  Each barrier wait gives up after about one
+// second (globaltimer), sets err and returns; a block that sees err set
+// returns at its next barrier, so the kernel always ends.
+// ---------------------------------------------------------------------------
+constexpr int PS_THREADS = LZ_THREADS;  // the finalisation order is k_fin's
+constexpr int PS_SLOTS = 32;            // tiles per block at most
+
+struct StepArgs {
+  const ll *tbeg, *tend;
+  const int *tgrp;
+  GState *gs;
+  void *p, *w, *V;
+  ll VS;
+  const unsigned *ell;
+  const ll *slice_off;
+  const int *slice_w;
+  double *part;  // 3 T: the P, SpMV and R tile partials
+  double *diagT, *upperT, *vnorm;
+  unsigned *bar;  // barrier arrivals (zero at launch)
+  int *run_cnt;   // per step: groups still running after it (zero at launch)
+  int *err;       // 2: a barrier wait gave up
+  int T, MI;
+  double tol;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__global__ void k_ps_reset(unsigned *__restrict__ bar, int *__restrict__ run_cnt, int MI) {
+  pdl_entry();
+  if (threadIdx.x == 0) bar[0] = 0u;
+  for (int i = threadIdx.x; i < MI; i += blockDim.x) run_cnt[i] = 0;
+}
+
+// Grid barrier number k (targets k G arrivals).  False when it gave up or
+// another block did.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    int ok = 1;
+    const unsigned long long t0 = global_ns();
+    for (unsigned n = 0;; n++) {
+      if (ld_acquire_u32(bar) >= target) break;
+      if (*(volatile int *)err) {
+        ok = 0;
+        break;
+      }
+      if ((n & 63) == 63 && (global_ns() - t0 > 1000000000ull || n > (1u << 26))) {
+        atomicExch(err, 2);  // about one second, or 2^26 polls of at least 64 ns
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  __threadfence();  // every thread: later loads see the other blocks' writes
+  return ok_s != 0;
+}
+
+// The step finalisation OP for every slot of the block whose group runs, in
+// k_fin's reduction order (256 threads: strided sequential sums, warp trees,
+// the warps in order).  A group of more than 256 tiles is reduced by the
+// whole block with k_fin's own code (eight loads in flight per thread); a
+// smaller one by one warp that stands in for the 256 threads (each holds at
+// most one partial), all of its loads issued before the trees.
+template <int OP>
+__device__ __forceinline__ void step_fin(GState *st, const int *sg, int nslot,
+                                         const double *__restrict__ part, const StepArgs &a,
+                                         int it, double *sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < nslot; k++) {  // big groups: the whole block
+    GState &s = st[k];
+    if (!s.run || s.ntiles <= PS_THREADS) continue;  // block-uniform
+    double acc = 0.0;
+    int q = threadIdx.x;
+    for (; q + 7 * PS_THREADS < s.ntiles; q += 8 * PS_THREADS) {
+      double x[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) x[u] = __ldcg(&part[s.tile0 + q + u * PS_THREADS]);
+#pragma unroll
+      for (int u = 0; u < 8; u++) acc = __dadd_rn(acc, x[u]);
+    }
+    for (; q < s.ntiles; q += PS_THREADS) acc = __dadd_rn(acc, __ldcg(&part[s.tile0 + q]));
+    const double tot = block_sum(acc, sh);
+    if (threadIdx.x == 0) {
+      const int t = blockIdx.x + k * gridDim.x;
+      fin_apply<OP>(s, sg[k], tot, 0.0, it, a.MI, a.tol, 0, a.diagT, a.upperT, a.vnorm, nullptr,
+                    t == s.tile0);
+    }
+    __syncthreads();
+  }
+  for (int k = warp; k < nslot; k += PS_THREADS / 32) {  // small groups: a warp each
+    GState &s = st[k];
+    if (!s.run || s.ntiles > PS_THREADS) continue;  // warp-uniform
+    double x[PS_THREADS / 32];
+#pragma unroll
+    for (int u = 0; u < PS_THREADS / 32; u++) {
+      const int q = lane + 32 * u;
+      x[u] = q < s.ntiles ? __dadd_rn(0.0, __ldcg(&part[s.tile0 + q])) : 0.0;
+    }
+    double tot = 0.0;
+#pragma unroll
+    for (int u = 0; u < PS_THREADS / 32; u++) {
+      const double ws = warp_tree_sum(x[u]);
+      if (lane == 0) tot = __dadd_rn(tot, ws);
+    }
+    if (lane == 0) {
+      const int t = blockIdx.x + k * gridDim.x;
+      fin_apply<OP>(s, sg[k], tot, 0.0, it, a.MI, a.tol, 0, a.diagT, a.upperT, a.vnorm, nullptr,
+                    t == s.tile0);
+    }
+  }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(PS_THREADS, 8) k_steps(StepArgs a) {
+  __shared__ GState st[PS_SLOTS];
+  __shared__ int sg[PS_SLOTS];
+  __shared__ double cs[LZ_TILE / 32 + 2];
+  __shared__ float2 cs2[LZ_TILE / 32 + 2];
+  __shared__ double wlut[16];
+  __shared__ double sh[32];
+  const int G = gridDim.x;
+  const int nslot = (a.T - (int)blockIdx.x + G - 1) / G;  // tiles blockIdx.x + k G < T
+  VT *p = static_cast<VT *>(a.p), *w = static_cast<VT *>(a.w), *V = static_cast<VT *>(a.V);
+  double *partP = a.part, *partS = a.part + a.T, *partR = a.part + 2 * (ll)a.T;
+  for (int k = threadIdx.x; k < nslot; k += PS_THREADS) {
+    sg[k] = a.tgrp[blockIdx.x + k * G];
+    st[k] = a.gs[sg[k]];
+  }
+  if (threadIdx.x < 16) wlut[threadIdx.x] = (double)threadIdx.x;
+  __syncthreads();
+  unsigned nbar = 0;
+  for (int it = 0; it < a.MI; it++) {
+    // p = r (step 0) or beta (p - c) + r; partials of sum p
+    for (int k = 0; k < nslot; k++) {
+      if (!st[k].run) continue;  // block-uniform
+      const int t = blockIdx.x + k * G;
+      pr_tile<VT, TM_P, 1>(a.tbeg[t], a.tend[t], (VT)st[k].c, (VT)st[k].beta, (VT)st[k].alpha,
+                           it, p, w, V, a.VS, cs, cs2, partP, t);
+      __syncthreads();
+    }
+    if (!grid_barrier(a.bar, ++nbar * (unsigned)G, a.err)) return;
+    if (it > 0 && ld_acquire_u32(reinterpret_cast<const unsigned *>(a.run_cnt) + it - 1) == 0)
+      break;  // no group of the level runs (the same value in every block)
+    step_fin<FIN_PMEAN>(st, sg, nslot, partP, a, it, sh);
+    __syncthreads();
+    // w = L p; partials of sum w (p - c)
+    for (int k = 0; k < nslot; k++) {
+      if (!st[k].run) continue;
+      const int t = blockIdx.x + k * G;
+      spmv_tile<VT>(a.tbeg[t], a.tend[t], (VT)st[k].c, a.ell, a.slice_off, a.slice_w, p, w, wlut,
+                    cs, cs2, partS, t);
+      __syncthreads();
+    }
+    if (!grid_barrier(a.bar, ++nbar * (unsigned)G, a.err)) return;
+    step_fin<FIN_PAP>(st, sg, nslot, partS, a, it, sh);
+    __syncthreads();
+    // V[it+1] = V[it] - alpha w; partials of sum V[it+1]^2
+    for (int k = 0; k < nslot; k++) {
+      if (!st[k].run) continue;
+      const int t = blockIdx.x + k * G;
+      pr_tile<VT, TM_R, 1>(a.tbeg[t], a.tend[t], (VT)st[k].c, (VT)st[k].beta, (VT)st[k].alpha,
+                           it, p, w, V, a.VS, cs, cs2, partR, t);
+      __syncthreads();
+    }
+    if (!grid_barrier(a.bar, ++nbar * (unsigned)G, a.err)) return;
+    step_fin<FIN_RTR>(st, sg, nslot, partR, a, it, sh);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int running = 0;
+      for (int k = 0; k < nslot; k++)
+        if (blockIdx.x + k * G == st[k].tile0 && st[k].run) running++;
+      if (running) atomicAdd(&a.run_cnt[it], running);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nslot; k += PS_THREADS)
+    if ((int)blockIdx.x + k * G == st[k].tile0) a.gs[sg[k]] = st[k];
 }
 
 // Ritz vector f_i = sum_j coef_j V_j[i] (j < iters, src/fiedler.c:520-535)
@@ -1615,6 +2018,15 @@ struct Lanczos {
   DBuf<long long> loop_ctr;      // device restart loop: passes, SpMV steps
   bool reorth = false;           // reorthogonalise every residual (opt-in)
   DBuf<double> part2, hro;       //   its tile partials and coefficients
+  // persistent step kernel (k_steps): with PARRSB_GPU_PERSIST=1, unless per-
+  // kernel timing, reorthogonalisation or a fused finalisation is asked for,
+  // and when the level's tiles fit its resident grid
+  bool persist = false;
+  int ps_grid = 0;               //   its blocks
+  DBuf<unsigned> ps_bar;         //   barrier arrivals
+  DBuf<int> ps_run;              //   groups still running after each step
+  DBuf<ll> fq;                   // fixed-point f of the residual check (FP32)
+  DBuf<unsigned> gmax, tmax;     //   each group's and tile's largest |f| (IEEE bits)
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
   double resid_tol = 0.0;        // its bound (rsb_tol); passes then use
   double cg_factor = 1.0;        //   tol * cg_factor for their own CG exit
@@ -1671,7 +2083,7 @@ struct Lanczos {
     h2d(tgrp.p, hg.data(), T);
     f.ensure(N), p.ensure(N), w.ensure(N);
     V.ensure((size_t)(MI + 1) * VS);
-    part.ensure((size_t)2 * T + 2);
+    part.ensure((size_t)3 * T + 2);
     diagT.ensure((size_t)A * MI), upperT.ensure((size_t)A * MI);
     vnorm.ensure((size_t)A * (MI + 1)), coef.ensure((size_t)A * MI);
     any.ensure(2);
@@ -1798,7 +2210,11 @@ struct Lanczos {
     tile<TM_INIT_R, GATE_ACTIVE>();
     fin<FIN_INIT_RTR, GATE_ACTIVE>(0, tol);
     mark(4 * MI + 1);
-    for (int it = 0; it < MI; it++) {
+    if (persist) {
+      steps_persistent(lv, tol);
+      *spmv_launches += MI;
+    }
+    for (int it = 0; it < (persist ? 0 : MI); it++) {
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
       mark(4 * it + 0);
@@ -1850,11 +2266,63 @@ struct Lanczos {
     } else {
       // restart until the Ritz vector's FP64 eigen-residual is at most tol
       fin<FIN_PASS_END_R, GATE_ACTIVE>(0, tol, mpass);
-      tile<TM_RESID1, GATE_ACTIVE>(0, &lv);
+      resid1<GATE_ACTIVE>(lv);
       fin<FIN_RESID1, GATE_ACTIVE>();
       tile<TM_RESID2, GATE_ACTIVE>(0, &lv);
       fin<FIN_RESID_GATE, GATE_ACTIVE>(0, resid_tol, mpass);
     }
+  }
+
+  // kernels of the steps of one pass
+  long long step_kernels() const {
+    if (persist) return 2;
+    return (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) +
+           (reorth ? 3ll * MI : 0);
+  }
+
+  // all steps of the pass in one cooperative launch (k_steps)
+  void steps_persistent(const Level &lv, double tol) {
+    cudaStream_t st = ctx().stream;
+    // (a kernel, not memset nodes, in front of the cooperative launch)
+    k_ps_reset<<<1, 128, 0, st>>>(ps_bar.p, ps_run.p, MI);
+    CK_LAUNCH();
+    StepArgs sa;
+    sa.tbeg = tbeg.p, sa.tend = tend.p, sa.tgrp = tgrp.p, sa.gs = gs.p;
+    sa.p = p.p, sa.w = w.p, sa.V = V.p, sa.VS = VS;
+    sa.ell = lv.ell.p, sa.slice_off = lv.slice_off.p, sa.slice_w = lv.slice_w.p;
+    sa.part = part.p;
+    sa.diagT = diagT.p, sa.upperT = upperT.p, sa.vnorm = vnorm.p;
+    sa.bar = ps_bar.p, sa.run_cnt = ps_run.p, sa.err = err.p;
+    sa.T = T, sa.MI = MI, sa.tol = tol;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ps_grid);
+    cfg.blockDim = dim3(PS_THREADS);
+    cfg.stream = st;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    ctx().kernel_launches++;
+    CK(cudaLaunchKernelEx(&cfg, k_steps<VT>, sa));
+  }
+
+  // whether this level runs its steps in k_steps, and with how many blocks
+  bool want_persist() {
+    const char *e = getenv("PARRSB_GPU_PERSIST");
+    if (!e || atoi(e) == 0) return false;  // opt-in
+    if (reorth || pr_fused || sp_fused || !ev.empty() || T <= 0) return false;
+    int dev = 0, sms = 0, per_sm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_steps<VT>, PS_THREADS, 0));
+    const ll cap = (ll)sms * per_sm;
+    if (cap <= 0) return false;
+    ps_grid = (int)std::min<ll>(T, cap);
+    if ((T + ps_grid - 1) / ps_grid > PS_SLOTS) return false;
+    ps_bar.ensure(1);
+    ps_run.ensure((size_t)MI);
+    return true;
   }
 
   // shared memory of one k_spmv_tma stage (nw slices of the widest width)
@@ -1939,7 +2407,7 @@ struct Lanczos {
            int start_kind = 0) {
     cudaStream_t st = ctx().stream;
     if (resid_stop) {
-      y64.ensure((size_t)N);
+      resid_bufs();
       resid_tol = tol;
       tol = tol * cg_factor;  // a pass's own CG exit
     }
@@ -1974,7 +2442,11 @@ struct Lanczos {
       return !(e && atoi(e) == 0);
     }();
     static bool device_loop_broken = false;
-    if (use_graph && ev.empty() && device_loop_env && !device_loop_broken) try {
+    static bool persist_broken = false;  // a graph with k_steps failed here once
+    persist = !persist_broken && want_persist();
+    for (int attempt = 0;
+         attempt < 2 && !exec && use_graph && ev.empty() && device_loop_env && !device_loop_broken;
+         attempt++) try {
       const auto h0 = std::chrono::steady_clock::now();
       CK(cudaGraphCreate(&graph, 0));
       cudaGraphConditionalHandle hnd;
@@ -2014,6 +2486,13 @@ struct Lanczos {
       if (exec) cudaGraphExecDestroy(exec);
       if (graph) cudaGraphDestroy(graph);
       exec = nullptr, graph = nullptr;
+      if (persist) {  // try again with the launch-per-kernel steps
+        persist_broken = true;
+        persist = false;
+        fprintf(stderr, "parrsb_gb300: persistent step kernel unavailable in graphs (%s)\n",
+                cudaGetErrorString(e.err));
+        continue;
+      }
       device_loop_broken = true;
       fprintf(stderr, "parrsb_gb300: device restart loop unavailable (%s); host loop used\n",
               cudaGetErrorString(e.err));
@@ -2025,8 +2504,7 @@ struct Lanczos {
       d2h(hc, loop_ctr.p, 2);
       sync();
       const long long per_pass_kernels =
-          6 + (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) + 5 +
-          (resid_stop ? 4 : 0) + (reorth ? 3ll * MI : 0);
+          6 + step_kernels() + 5 + (resid_stop ? 3 + resid1_launches(lv) : 0);
       ctx().kernel_launches += per_pass_kernels * hc[0];
       ctx().stats.lanczos_passes += hc[0];
       ctx().stats.spmv_launches += hc[1];
@@ -2039,7 +2517,7 @@ struct Lanczos {
       finish_run();
       return;
     }
-    if (use_graph) {
+    for (int attempt = 0; attempt < 2 && use_graph && !exec; attempt++) try {
       const auto h0 = std::chrono::steady_clock::now();
       CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
       long long kl = ctx().kernel_launches;
@@ -2049,10 +2527,25 @@ struct Lanczos {
       CK(cudaGraphInstantiate(&exec, graph, 0));
       ctx().stats.lanczos_host_ms[1] +=
           std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+    } catch (const CudaError &e) {
+      if (!persist) throw;
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+        cudaGraph_t g2 = nullptr;
+        cudaStreamEndCapture(st, &g2);
+        if (g2) cudaGraphDestroy(g2);
+      }
+      cudaGetLastError();
+      if (exec) cudaGraphExecDestroy(exec);
+      if (graph) cudaGraphDestroy(graph);
+      exec = nullptr, graph = nullptr;
+      persist_broken = true;
+      persist = false;
+      fprintf(stderr, "parrsb_gb300: persistent step kernel unavailable in graphs (%s)\n",
+              cudaGetErrorString(e.err));
     }
     const long long per_pass_kernels =
-        4 + (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) + 5 +
-        (resid_stop ? 4 : 0) + (reorth ? 3ll * MI : 0);
+        4 + step_kernels() + 5 + (resid_stop ? 3 + resid1_launches(lv) : 0);
     launches = 0;
     // PARRSB_GPU_LEVEL_LOG=1 (timing mode): one line per level on stderr
     const bool level_log = !ev.empty() && getenv("PARRSB_GPU_LEVEL_LOG");
@@ -2130,9 +2623,42 @@ struct Lanczos {
     tile<TM_SCALE_F, GATE_ALL>();
   }
 
-  void residual(const Level &lv) {
+  // y64 = L f and the tile partials of f.y and f.f, for FIN_RESID1: the
+  // exact fixed-point form for FP32 vectors (k_rq_*), else FP64 (k_tile)
+  bool resid_int(const Level &lv) const { return sizeof(VT) == 4 && lv.max_w <= RQ_MAX_WIDTH; }
+  // Buffers of the residual check.  Every buffer a pass graph uses must
+  // exist before its capture starts: an allocation from the stream-ordered
+  // pool on a capturing stream becomes a node of the graph (memory the graph
+  // owns, not allowed in a conditional body at all).
+  void resid_bufs() {
     y64.ensure((size_t)N);
-    tile<TM_RESID1, GATE_ALL>(0, &lv);
+    if (sizeof(VT) == 4) {
+      fq.ensure((size_t)N);
+      gmax.ensure((size_t)A);
+      tmax.ensure((size_t)T);
+    }
+  }
+  int resid1_launches(const Level &lv) const { return resid_int(lv) ? 3 : 1; }
+  template <int GATE>
+  void resid1(const Level &lv) {
+    if constexpr (sizeof(VT) == 4) {
+      if (resid_int(lv)) {
+        cudaStream_t st = ctx().stream;
+        resid_bufs();  // (allocated before any capture: a no-op here then)
+        launch_pdl(k_rq_max<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, tmax.p);
+        launch_pdl(k_rq_quant<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, tmax.p,
+                   gmax.p, fq.p);
+        launch_pdl(k_rq_resid1<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, fq.p,
+                   gmax.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, y64.p, part.p);
+        return;
+      }
+    }
+    tile<TM_RESID1, GATE>(0, &lv);
+  }
+
+  void residual(const Level &lv) {
+    resid_bufs();
+    resid1<GATE_ALL>(lv);
     fin<FIN_RESID1, GATE_ALL>();
     tile<TM_RESID2, GATE_ALL>(0, &lv);
     fin<FIN_RESID2, GATE_ALL>();

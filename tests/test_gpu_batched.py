@@ -71,3 +71,20 @@ def test_batched_fp32(monkeypatch, mesh):
         m = seg == g
         if m.sum() > 100:
             assert abs(abs(f32[m] @ f64[m]) - 1.0) < 1e-3
+
+
+def test_fp32_residual_check_matches_fp64(oracle, monkeypatch, mesh):
+    """With FP32 vectors the residual check computes L f exactly in 64-bit
+    fixed point: the reported ||L f - rho f|| / ||f|| of every returned
+    vector equals the FP64 value computed from that vector to 1e-8."""
+    vtx, xyz, seg = mesh
+    ng = int(seg.max()) + 1
+    monkeypatch.setenv("PARRSB_GPU_FP32", "1")
+    f, _, rs = P.fiedler_groups(vtx, seg, ng)
+    for g in range(ng):
+        m = seg == g
+        fg = f[m]
+        y = oracle.laplacian(fg, vtx[m])
+        rho = (fg @ y) / (fg @ fg)
+        ro = np.linalg.norm(y - rho * fg) / np.linalg.norm(fg)
+        assert abs(rs[g] - ro) <= 1e-8 * ro + 1e-13, (g, rs[g], ro)

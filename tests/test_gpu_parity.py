@@ -235,7 +235,6 @@ def test_rsb_staged_spmv_bitwise(monkeypatch, shape, nparts):
     np.testing.assert_array_equal(a, b)
 
 
-
 @pytest.mark.parametrize("partitioner", [0, 1])
 def test_pinned_host_buffers_same_partition(partitioner):
     """parrsb_part_mesh with page-locked host buffers, called twice on the
@@ -392,3 +391,46 @@ def test_device_restart_loop_same_bits(monkeypatch, stop):
     assert sa.lanczos_iters == sb.lanczos_iters
     assert sa.lanczos_passes == sb.lanczos_passes
     assert sa.spmv_launches == sb.spmv_launches
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+@pytest.mark.parametrize("mode", ["device_loop", "host_loop", "no_graphs"])
+def test_persistent_steps_bitwise(monkeypatch, fp32, mode):
+    """All steps of a pass in one cooperative launch (k_steps, grid barriers
+    between the phases) give bitwise the partition, the step counts and the
+    eigen-residuals of one launch per kernel, inside the device restart
+    loop's graph, in a per-pass graph and without graphs."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", fp32)
+    monkeypatch.setenv("PARRSB_GPU_RESID_STOP", "1")
+    if mode == "host_loop":
+        monkeypatch.setenv("PARRSB_GPU_DEVICE_LOOP", "0")
+    if mode == "no_graphs":
+        monkeypatch.setenv("PARRSB_GPU_GRAPHS", "0")
+    vtx, xyz = meshgen.box_hex(40, 36, 20, jitter=0.1, seed=21)
+    out, launches = [], []
+    for ps in ("0", "1"):
+        monkeypatch.setenv("PARRSB_GPU_PERSIST", ps)
+        part = P.part_mesh(vtx, xyz, 32, partitioner=0)
+        st = P.last_stats()
+        out.append((part, st.lanczos_iters, st.lanczos_row_iters, st.max_fiedler_resid,
+                    list(st.level_steps)))
+        launches.append(st.kernel_launches)
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1:] == out[1][1:]
+    assert launches[1] < launches[0] // 2  # the steps ran in k_steps
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+def test_persistent_steps_many_tiles_per_block(monkeypatch, fp32):
+    """More tiles than resident blocks (each block owns several tiles of
+    different groups): the Fiedler vectors and step counts of 600 ragged
+    subgraphs equal bitwise those of the launch-per-kernel steps."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", fp32)
+    vtx, _, seg = meshgen.subboxes(600, smin=200, smax=3000, delete=0.05, seed=9)
+    ng = int(seg.max()) + 1
+    res = []
+    for ps in ("0", "1"):
+        monkeypatch.setenv("PARRSB_GPU_PERSIST", ps)
+        res.append(P.fiedler_groups(vtx, seg, ng, batched=True))
+    for a, b in zip(res[0], res[1]):
+        np.testing.assert_array_equal(a, b)
