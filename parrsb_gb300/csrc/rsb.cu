@@ -2196,9 +2196,17 @@ struct Lanczos {
 
   // One Lanczos pass (restart) for the active groups: the body that the
   // CUDA graph captures.
+  // event record inside a pass: an external event node while the pass is
+  // captured, a plain record when it runs without a graph
+  void record(cudaEvent_t e) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(ctx().stream, &cs));
+    CK(cudaEventRecordWithFlags(
+        e, ctx().stream,
+        cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault));
+  }
   void mark(int k) {
-    if (!evk.empty())
-      CK(cudaEventRecordWithFlags(evk[k], ctx().stream, cudaEventRecordExternal));
+    if (!evk.empty()) record(evk[k]);
   }
   // evk layout: [4 it .. 4 it + 3] p start/stop, r start/stop of step it;
   // then 4 MI + 0..5: init start/stop, eig start/stop, ritz start/stop
@@ -2228,10 +2236,10 @@ struct Lanczos {
         fin<FIN_PMEAN, GATE_RUN>(it, tol, mpass);
       }
       mark(4 * it + 1);
-      if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it], st, cudaEventRecordExternal));
+      if (!ev.empty()) record(ev[2 * it]);
       spmv(lv, sp_kind, bd, fargs(it, tol, mpass), sp_fused ? 1 : 0, 0);
       if (!sp_fused) fin<FIN_PAP, GATE_RUN>(it, tol, mpass);
-      if (!ev.empty()) CK(cudaEventRecordWithFlags(ev[2 * it + 1], st, cudaEventRecordExternal));
+      if (!ev.empty()) record(ev[2 * it + 1]);
       (*spmv_launches)++;
       mark(4 * it + 2);
       if (pr_fused && !reorth) {

@@ -434,3 +434,19 @@ def test_persistent_steps_many_tiles_per_block(monkeypatch, fp32):
         res.append(P.fiedler_groups(vtx, seg, ng, batched=True))
     for a, b in zip(res[0], res[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("graphs", ["0", "1"])
+def test_timing_mode_same_partition(monkeypatch, graphs):
+    """Per-kernel CUDA-event timing (PARRSB_GPU_TIMING=1), with per-pass
+    graphs or without graphs, gives the partition of the untimed call and
+    fills the SpMV and vector-update times."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", "1")
+    monkeypatch.setenv("PARRSB_GPU_GRAPHS", graphs)
+    vtx, xyz = meshgen.box_hex(24, 20, 16, jitter=0.1, seed=6)
+    a = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    monkeypatch.setenv("PARRSB_GPU_TIMING", "1")
+    b = P.part_mesh(vtx, xyz, 8, partitioner=0)
+    st = P.last_stats()
+    np.testing.assert_array_equal(a, b)
+    assert st.spmv_ms > 0 and st.lanczos_ms[0] > 0 and st.lanczos_ms[1] > 0
