@@ -331,7 +331,7 @@ __device__ __forceinline__ void fin_apply(GState &s, int g, double tot0, double 
 // threads) and apply the scalar update OP.  Run by a whole block: either the
 // dedicated k_fin launch or, fused, the last tile block of the group to
 // finish.
-template <int OP>
+template <int OP, bool WIDE = false>
 __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int it, int MI,
                          double tol, int mpass, double *__restrict__ diagT,
                          double *__restrict__ upperT, double *__restrict__ vnorm,
@@ -342,15 +342,29 @@ __device__ void fin_body(GState &s, int g, const double *__restrict__ part, int 
     for (int v = 0; v < nv; v++) {
       double acc = 0.0;
       const int bd = blockDim.x;
-      int q = threadIdx.x;
-      for (; q + 7 * bd < s.ntiles; q += 8 * bd) {  // eight loads in flight, same order
-        double x[8];
+      if (WIDE) {  // up to eight loads in flight per thread, then the adds in order
+        for (int q = threadIdx.x; q < s.ntiles; q += 8 * bd) {
+          double x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) x[u] = __ldcg(&part[(ll)nv * (s.tile0 + q + u * bd) + v]);
+          for (int u = 0; u < 8; u++)
+            x[u] = q + u * bd < s.ntiles ? __ldcg(&part[(ll)nv * (s.tile0 + q + u * bd) + v])
+                                         : 0.0;
 #pragma unroll
-        for (int u = 0; u < 8; u++) acc = __dadd_rn(acc, x[u]);
+          for (int u = 0; u < 8; u++)
+            if (q + u * bd < s.ntiles) acc = __dadd_rn(acc, x[u]);
+        }
+      } else {  // the same adds with fewer registers (inlined into the tile kernels)
+        int q = threadIdx.x;
+        for (; q + 7 * bd < s.ntiles; q += 8 * bd) {
+          double x[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) x[u] = __ldcg(&part[(ll)nv * (s.tile0 + q + u * bd) + v]);
+#pragma unroll
+          for (int u = 0; u < 8; u++) acc = __dadd_rn(acc, x[u]);
+        }
+        for (; q < s.ntiles; q += bd)
+          acc = __dadd_rn(acc, __ldcg(&part[(ll)nv * (s.tile0 + q) + v]));
       }
-      for (; q < s.ntiles; q += bd) acc = __dadd_rn(acc, __ldcg(&part[(ll)nv * (s.tile0 + q) + v]));
       tot[v] = block_sum(acc, sh);
       __syncthreads();
     }
@@ -457,7 +471,7 @@ __global__ void k_fin(GState *__restrict__ gs, int ngroups, const double *__rest
   if (g >= ngroups) return;
   GState &s = gs[g];
   if (!gate_ok(s, GATE)) return;
-  fin_body<OP>(s, g, part, it, MI, tol, mpass, diagT, upperT, vnorm, any_active, sh);
+  fin_body<OP, true>(s, g, part, it, MI, tol, mpass, diagT, upperT, vnorm, any_active, sh);
 }
 
 // Fused finalisation: after a tile block has written its partial, the last
@@ -705,10 +719,14 @@ k_tile(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
 // 2^-22 of the group's largest are exact; smaller ones lose at most
 // 2^-47 of it).  Then y_i = d_i Fq_i - sum_j w_ij Fq_j is exact in int64
 // for rows of fewer than 2048 stored entries (|terms| < 2^51 each) and is
-// rounded once to FP64.  The sums f.y and f.f and their reduction order are
-// those of the FP64 form (TM_RESID1 of k_tile).
+// rounded once to FP64.  The sums f.y, f.f and (y - rho f)^2 stay FP64 but
+// each lane first accumulates its own rows (one FMA per row and sum) before
+// one warp tree per warp: a tree per 32-row chunk, as k_tile's FP64 form
+// does, costs five more FP64 adds per row, and the FP64 pipe, not the
+// gathers, bounded that form.
 // ---------------------------------------------------------------------------
 constexpr int RQ_MAX_WIDTH = 2048;  // widest ELL slice the integer form accepts
+constexpr int RQ_THREADS = 256;     // the tile sums' order depends on it
 
 // per tile: the largest |f| of the tile's rows (IEEE bits, which order like
 // the magnitudes)
@@ -775,7 +793,7 @@ k_rq_quant(const ll *__restrict__ tbeg, const ll *__restrict__ tend, const int *
 }
 
 template <int GATE>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(RQ_THREADS)
 k_rq_resid1(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
             const int *__restrict__ tgrp, const GState *__restrict__ gs,
             const float *__restrict__ f, const ll *__restrict__ fq,
@@ -783,7 +801,7 @@ k_rq_resid1(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
             const ll *__restrict__ slice_off, const int *__restrict__ slice_w,
             double *__restrict__ y64, double *__restrict__ part) {
   pdl_entry();
-  __shared__ double cs[2][LZ_TILE / 32 + 1];
+  __shared__ double cs[2][RQ_THREADS / 32];
   const int t = blockIdx.x, g = tgrp[t];
   if (!gate_ok(gs[g], GATE)) return;
   const unsigned gm = gmax[g];
@@ -792,54 +810,83 @@ k_rq_resid1(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
   const bool finite = gm < 0x7F800000u;
   const double unscale =
       __longlong_as_double((ll)(1023 - 46 + ((int)(gm >> 23) - 127)) << 52);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const ll b = tbeg[t], e = tend[t];
   const ll c0 = b >> 5;
   const int nc = (int)(((e - 1) >> 5) - c0 + 1);
-  for (int q = warp; q < nc; q += nw) {
+  double a1 = 0.0, a2 = 0.0;  // this lane's f.y and f.f over its rows, in slice order
+  for (int q = warp; q < nc; q += RQ_THREADS / 32) {
     const ll i = (c0 + q) * 32 + lane;
-    const bool valid = i >= b && i < e;
-    double d1 = 0.0, d2 = 0.0;
-    if (valid) {
-      const ll sl = i >> 5;
-      const unsigned *ep = ell + slice_off[sl] + (i & 31);
-      const int wd = slice_w[sl];
-      ll acc = 0;
-      int dsum = 0;
-      int k = 0;
+    if (i < b || i >= e) continue;
+    const ll sl = i >> 5;
+    const unsigned *ep = ell + slice_off[sl] + (i & 31);
+    const int wd = slice_w[sl];
+    ll acc = 0;
+    int dsum = 0;
+    int k = 0;
 #pragma unroll 1
-      for (; k + 8 <= wd; k += 8) {
-        unsigned x[8];
+    for (; k + 8 <= wd; k += 8) {
+      unsigned x[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) x[u] = __ldcs(ep + (ll)(k + u) * 32);
-        ll fj[8];
+      for (int u = 0; u < 8; u++) x[u] = __ldcs(ep + (ll)(k + u) * 32);
+      ll fj[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++) fj[u] = fq[x[u] & 0x0FFFFFFFu];
+      for (int u = 0; u < 8; u++) fj[u] = fq[x[u] & 0x0FFFFFFFu];
 #pragma unroll
-        for (int u = 0; u < 8; u++) {
-          acc += (ll)(x[u] >> 28) * fj[u];
-          dsum += (int)(x[u] >> 28);
-        }
+      for (int u = 0; u < 8; u++) {
+        acc += (ll)(x[u] >> 28) * fj[u];
+        dsum += (int)(x[u] >> 28);
       }
-      for (; k < wd; k++) {
-        const unsigned x = __ldcs(ep + (ll)k * 32);
-        acc += (ll)(x >> 28) * fq[x & 0x0FFFFFFFu];
-        dsum += (int)(x >> 28);
-      }
-      const ll yq = (ll)dsum * fq[i] - acc;
-      const double yv = finite ? __dmul_rn(__ll2double_rn(yq), unscale) : __longlong_as_double(0x7FF8000000000000ll);
-      y64[i] = yv;
-      const double fi = (double)f[i];
-      d1 = __dmul_rn(fi, yv);
-      d2 = __dmul_rn(fi, fi);
     }
-    const double v1 = warp_tree_sum(d1), v2 = warp_tree_sum(d2);
-    if (lane == 0) cs[0][q] = v1, cs[1][q] = v2;
+    for (; k < wd; k++) {
+      const unsigned x = __ldcs(ep + (ll)k * 32);
+      acc += (ll)(x >> 28) * fq[x & 0x0FFFFFFFu];
+      dsum += (int)(x >> 28);
+    }
+    const ll yq = (ll)dsum * fq[i] - acc;
+    const double yv = finite ? __dmul_rn(__ll2double_rn(yq), unscale)
+                             : __longlong_as_double(0x7FF8000000000000ll);
+    y64[i] = yv;
+    const double fi = (double)f[i];
+    a1 = __fma_rn(fi, yv, a1);
+    a2 = __fma_rn(fi, fi, a2);  // fi * fi is exact
   }
+  const double v1 = warp_tree_sum(a1), v2 = warp_tree_sum(a2);
+  if (lane == 0) cs[0][warp] = v1, cs[1][warp] = v2;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    const double v0 = tile_total(cs[0], nc), v1 = tile_total(cs[1], nc);
-    if (threadIdx.x == 0) part[2 * t] = v0, part[2 * t + 1] = v1;
+  if (threadIdx.x == 0) {
+    double s1 = 0.0, s2 = 0.0;
+    for (int w = 0; w < RQ_THREADS / 32; w++) s1 = __dadd_rn(s1, cs[0][w]), s2 = __dadd_rn(s2, cs[1][w]);
+    part[2 * t] = s1, part[2 * t + 1] = s2;
+  }
+}
+
+// sum (y - rho f)^2 per tile for the FP32 residual check (rho in the group
+// state's c): a thread's rows in order, warp trees, the warps in order
+template <int GATE>
+__global__ void __launch_bounds__(RQ_THREADS)
+k_rq_resid2(const ll *__restrict__ tbeg, const ll *__restrict__ tend,
+            const int *__restrict__ tgrp, const GState *__restrict__ gs,
+            const float *__restrict__ f, const double *__restrict__ y64,
+            double *__restrict__ part) {
+  pdl_entry();
+  __shared__ double cs[RQ_THREADS / 32];
+  const int t = blockIdx.x, g = tgrp[t];
+  const GState &s = gs[g];
+  if (!gate_ok(s, GATE)) return;
+  const double rho = s.c;
+  double a = 0.0;
+  for (ll i = tbeg[t] + threadIdx.x; i < tend[t]; i += RQ_THREADS) {
+    const double v = __fma_rn(-rho, (double)f[i], y64[i]);
+    a = __fma_rn(v, v, a);
+  }
+  const double w = warp_tree_sum(a);
+  if ((threadIdx.x & 31) == 0) cs[threadIdx.x >> 5] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s1 = 0.0;
+    for (int k = 0; k < RQ_THREADS / 32; k++) s1 = __dadd_rn(s1, cs[k]);
+    part[t] = s1;
   }
 }
 
@@ -1405,15 +1452,15 @@ __device__ __forceinline__ void step_fin(GState *st, const int *sg, int nslot,
     GState &s = st[k];
     if (!s.run || s.ntiles <= PS_THREADS) continue;  // block-uniform
     double acc = 0.0;
-    int q = threadIdx.x;
-    for (; q + 7 * PS_THREADS < s.ntiles; q += 8 * PS_THREADS) {
+    for (int q = threadIdx.x; q < s.ntiles; q += 8 * PS_THREADS) {  // as fin_body
       double x[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) x[u] = __ldcg(&part[s.tile0 + q + u * PS_THREADS]);
+      for (int u = 0; u < 8; u++)
+        x[u] = q + u * PS_THREADS < s.ntiles ? __ldcg(&part[s.tile0 + q + u * PS_THREADS]) : 0.0;
 #pragma unroll
-      for (int u = 0; u < 8; u++) acc = __dadd_rn(acc, x[u]);
+      for (int u = 0; u < 8; u++)
+        if (q + u * PS_THREADS < s.ntiles) acc = __dadd_rn(acc, x[u]);
     }
-    for (; q < s.ntiles; q += PS_THREADS) acc = __dadd_rn(acc, __ldcg(&part[s.tile0 + q]));
     const double tot = block_sum(acc, sh);
     if (threadIdx.x == 0) {
       const int t = blockIdx.x + k * gridDim.x;
@@ -2276,7 +2323,7 @@ struct Lanczos {
       fin<FIN_PASS_END_R, GATE_ACTIVE>(0, tol, mpass);
       resid1<GATE_ACTIVE>(lv);
       fin<FIN_RESID1, GATE_ACTIVE>();
-      tile<TM_RESID2, GATE_ACTIVE>(0, &lv);
+      resid2<GATE_ACTIVE>(lv);
       fin<FIN_RESID_GATE, GATE_ACTIVE>(0, resid_tol, mpass);
     }
   }
@@ -2656,19 +2703,31 @@ struct Lanczos {
         launch_pdl(k_rq_max<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, tmax.p);
         launch_pdl(k_rq_quant<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, tmax.p,
                    gmax.p, fq.p);
-        launch_pdl(k_rq_resid1<GATE>, T, 256, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p, fq.p,
-                   gmax.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, y64.p, part.p);
+        launch_pdl(k_rq_resid1<GATE>, T, RQ_THREADS, 0, st, tbeg.p, tend.p, tgrp.p, gs.p, f.p,
+                   fq.p, gmax.p, lv.ell.p, lv.slice_off.p, lv.slice_w.p, y64.p, part.p);
         return;
       }
     }
     tile<TM_RESID1, GATE>(0, &lv);
+  }
+  // the tile partials of sum (y - rho f)^2, for FIN_RESID2 / FIN_RESID_GATE
+  template <int GATE>
+  void resid2(const Level &lv) {
+    if constexpr (sizeof(VT) == 4) {
+      if (resid_int(lv)) {
+        launch_pdl(k_rq_resid2<GATE>, T, RQ_THREADS, 0, ctx().stream, tbeg.p, tend.p, tgrp.p,
+                   gs.p, f.p, y64.p, part.p);
+        return;
+      }
+    }
+    tile<TM_RESID2, GATE>(0, &lv);
   }
 
   void residual(const Level &lv) {
     resid_bufs();
     resid1<GATE_ALL>(lv);
     fin<FIN_RESID1, GATE_ALL>();
-    tile<TM_RESID2, GATE_ALL>(0, &lv);
+    resid2<GATE_ALL>(lv);
     fin<FIN_RESID2, GATE_ALL>();
   }
 
