@@ -990,6 +990,336 @@ void compute_centroids(const double *xyz, int nel, int nv, double *cent) {
   CK_LAUNCH();
 }
 
+// ---------------------------------------------------------------------------
+// RCB on presorted coordinate lists, used when every axis rank is unique (no
+// two centroids share a coordinate on any axis).  Then a stable sort of a
+// segment by its axis rank does not depend on the segment's current order,
+// so each level needs no sort: every segment keeps, per axis a, the list of
+// its elements in increasing rank a (lists[a], in the segment's positions).
+// Its box is the ranks of the first and last entry of each list; its cut
+// sends the first `split` entries of the cut axis' list to the lower child;
+// the other lists are partitioned stably by that side (a segmented prefix
+// count, no comparison).  The tree, the cuts and the final order are those
+// of the sort-per-level path (the order of a segment that is not cut again
+// is its list along the axis of the cut that made it).  A level moves about
+// 130 B per element instead of four or five radix passes.
+// ---------------------------------------------------------------------------
+constexpr int PS_THREADS = 1024, PS_ITEMS = 4, PS_TILE = PS_THREADS * PS_ITEMS;
+
+// per segment: cut axis (-1: not cut at this level) and the lower child's size
+__global__ void k_ps_axis(const int *__restrict__ lists, const u32 *__restrict__ rank,
+                          const double *__restrict__ uniq, ll N, int ndim,
+                          const ll *__restrict__ st, const ll *__restrict__ n,
+                          const int *__restrict__ p, ll nseg, int do_local,
+                          int *__restrict__ axis, ll *__restrict__ split) {
+  const ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  if (!seg_active(p[s], n[s], do_local)) {
+    axis[s] = -1;
+    split[s] = n[s];
+    return;
+  }
+  double len[3] = {0.0, 0.0, 0.0};
+  if (n[s] > 0)
+    for (int d = 0; d < ndim; d++) {
+      const u32 lo = rank[(ll)d * N + lists[(ll)d * N + st[s]]];
+      const u32 hi = rank[(ll)d * N + lists[(ll)d * N + st[s] + n[s] - 1]];
+      len[d] = __dsub_rn(uniq[(ll)d * N + hi], uniq[(ll)d * N + lo]);
+    }
+  int ax = 0;
+  for (int d = 1; d < ndim; d++)
+    if (len[d] > len[ax]) ax = d;  // strictly longer wins: ties keep the lower axis
+  axis[s] = ax;
+  split[s] = p[s] > 1 ? lower_count(n[s], p[s]) : n[s] / 2;
+}
+
+// side of every element of a cut segment: 1 for the upper child
+__global__ void k_ps_side(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
+                          const ll *__restrict__ st, const int *__restrict__ axis,
+                          const ll *__restrict__ split, unsigned char *__restrict__ side) {
+  const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int s = seg_of_pos[j];
+  const int a = axis[s];
+  if (a < 0) return;
+  side[lists[(ll)a * N + j]] = (j - st[s]) >= split[s] ? 1 : 0;
+}
+
+// lower-child flag of list b's entry j (an uncut segment counts as lower:
+// its entries keep their places)
+__device__ __forceinline__ int ps_low(const int *__restrict__ lists, ll N, int b, ll j,
+                                      const int *__restrict__ seg_of_pos,
+                                      const int *__restrict__ axis,
+                                      const unsigned char *__restrict__ side) {
+  if (j >= N) return 0;
+  const int s = seg_of_pos[j];
+  if (axis[s] < 0) return 1;
+  return side[lists[(ll)b * N + j]] == 0 ? 1 : 0;
+}
+
+__device__ __forceinline__ int ps_block_excl(int v, int *total) {
+  __shared__ int ws[PS_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int t = lane < PS_THREADS / 32 ? ws[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < PS_THREADS / 32) ws[lane] = t;
+  }
+  __syncthreads();
+  const int excl = (warp ? ws[warp - 1] : 0) + x - v;
+  *total = ws[PS_THREADS / 32 - 1];
+  __syncthreads();
+  return excl;
+}
+
+// per list (blockIdx.y) and tile of PS_TILE positions: the count of lower flags
+__global__ void __launch_bounds__(PS_THREADS)
+k_ps_bsum(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
+          const int *__restrict__ axis, const unsigned char *__restrict__ side,
+          int *__restrict__ bsum, int nblk) {
+  const int b = blockIdx.y;
+  const ll j0 = (ll)blockIdx.x * PS_TILE + (ll)threadIdx.x * PS_ITEMS;
+  int c = 0;
+#pragma unroll
+  for (int k = 0; k < PS_ITEMS; k++) c += ps_low(lists, N, b, j0 + k, seg_of_pos, axis, side);
+  int total;
+  ps_block_excl(c, &total);
+  if (threadIdx.x == 0) bsum[(ll)b * nblk + blockIdx.x] = total;
+}
+
+// per list (blockIdx.x): exclusive scan of its tiles' counts, in place
+__global__ void __launch_bounds__(PS_THREADS) k_ps_bscan(int *__restrict__ bsum, int nblk) {
+  int *v = bsum + (ll)blockIdx.x * nblk;
+  const int per = (nblk + PS_THREADS - 1) / PS_THREADS;
+  const int i0 = threadIdx.x * per;
+  int c = 0;
+  for (int k = 0; k < per; k++)
+    if (i0 + k < nblk) c += v[i0 + k];
+  int total;
+  int run = ps_block_excl(c, &total);
+  for (int k = 0; k < per; k++)
+    if (i0 + k < nblk) {
+      const int x = v[i0 + k];
+      v[i0 + k] = run;
+      run += x;
+    }
+}
+
+// per list and position: the number of lower flags before it (exclusive)
+__global__ void __launch_bounds__(PS_THREADS)
+k_ps_prefix(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
+            const int *__restrict__ axis, const unsigned char *__restrict__ side,
+            const int *__restrict__ bsum, int nblk, int *__restrict__ clg) {
+  const int b = blockIdx.y;
+  const ll j0 = (ll)blockIdx.x * PS_TILE + (ll)threadIdx.x * PS_ITEMS;
+  int f[PS_ITEMS], c = 0;
+#pragma unroll
+  for (int k = 0; k < PS_ITEMS; k++)
+    f[k] = ps_low(lists, N, b, j0 + k, seg_of_pos, axis, side), c += f[k];
+  int total;
+  int run = ps_block_excl(c, &total) + bsum[(ll)b * nblk + blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < PS_ITEMS; k++) {
+    if (j0 + k < N) clg[(ll)b * N + j0 + k] = run;
+    run += f[k];
+  }
+}
+
+// stable partition of every cut segment of list b by side
+__global__ void k_ps_scatter(const int *__restrict__ lists, ll N, int ndim,
+                             const int *__restrict__ seg_of_pos, const ll *__restrict__ st,
+                             const int *__restrict__ axis, const ll *__restrict__ split,
+                             const unsigned char *__restrict__ side,
+                             const int *__restrict__ clg, int *__restrict__ lists2) {
+  const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int s = seg_of_pos[j];
+  const ll s0 = st[s];
+  for (int b = 0; b < ndim; b++) {
+    const int e = lists[(ll)b * N + j];
+    ll dest = j;
+    if (axis[s] >= 0) {
+      const ll c = clg[(ll)b * N + j] - clg[(ll)b * N + s0];  // lower entries before j
+      dest = side[e] == 0 ? s0 + c : s0 + split[s] + (j - s0 - c);
+    }
+    lists2[(ll)b * N + dest] = e;
+  }
+}
+
+// the axis whose list orders each child: the cut's axis, or the parent's
+__global__ void k_ps_oaxis(const int *__restrict__ axis, const int *__restrict__ oax, ll nseg,
+                           const ll *__restrict__ off, int *__restrict__ oax2) {
+  const ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const ll o = off[s];
+  if (axis[s] >= 0)
+    oax2[o] = oax2[o + 1] = axis[s];
+  else
+    oax2[o] = oax[s];
+}
+
+__global__ void k_ps_seg_keys(const int *__restrict__ sorted, const int *__restrict__ seg_of_elem,
+                              ll N, u64 *__restrict__ keys, int *__restrict__ vals) {
+  const ll r = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const int e = sorted[r];
+  keys[r] = (u64)(unsigned)seg_of_elem[e];
+  vals[r] = e;
+}
+
+__global__ void k_ps_seg_of_elem(const int *__restrict__ perm, const int *__restrict__ seg_of_pos,
+                                 ll N, int *__restrict__ seg_of_elem) {
+  const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < N) seg_of_elem[perm[j]] = seg_of_pos[j];
+}
+
+__global__ void k_ps_final(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
+                           const int *__restrict__ oax, int *__restrict__ perm) {
+  const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  const int a = oax[seg_of_pos[j]];
+  if (a >= 0) perm[j] = lists[(ll)a * N + j];
+}
+
+static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_local,
+                          int *part_of_elem, BisectWs &ws) {
+  cudaStream_t st = ctx().stream;
+  const ll n3 = (ll)ndim * N;
+  ws.lists.ensure((size_t)n3);
+  ws.lists2.ensure((size_t)n3);
+  ws.clg.ensure((size_t)n3);
+  ws.side.ensure((size_t)N);
+  // lists of the initial segments: the global rank order of each axis,
+  // grouped stably by segment
+  fill_seg_of_pos(t, ws.seg_of_pos.p, N);
+  if (t.count == 1) {
+    CK(cudaMemcpyAsync(ws.lists.p, ws.sorted.p, (size_t)n3 * sizeof(int),
+                       cudaMemcpyDeviceToDevice, st));
+  } else {
+    k_ps_seg_of_elem<<<grid_for(N, 256), 256, 0, st>>>(perm.p, ws.seg_of_pos.p, N,
+                                                        ws.seg_of_elem.p);
+    CK_LAUNCH();
+    for (int a = 0; a < ndim; a++) {
+      k_ps_seg_keys<<<grid_for(N, 256), 256, 0, st>>>(ws.sorted.p + (ll)a * N, ws.seg_of_elem.p,
+                                                      N, ws.keys.p, ws.vals.p);
+      CK_LAUNCH();
+      seg_sort_pairs(ws.keys, ws.vals, N, nullptr, 1, ws.sort);
+      CK(cudaMemcpyAsync(ws.lists.p + (ll)a * N, ws.vals.p, (size_t)N * sizeof(int),
+                         cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  ws.oax.ensure((size_t)t.count);
+  CK(cudaMemsetAsync(ws.oax.p, 0xFF, (size_t)t.count * sizeof(int), st));  // -1: input order
+  const int nblk = (int)((N + PS_TILE - 1) / PS_TILE);
+  ws.bsum.ensure((size_t)ndim * nblk);
+  DBuf<int> nact_d(1);
+  DBuf<unsigned long long> maxn_d(1);
+  for (int level = 0; level < 200; level++) {
+    const ll nseg = t.count;
+    ws.child_cnt.ensure((size_t)nseg);
+    CK(cudaMemsetAsync(nact_d.p, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(maxn_d.p, 0, sizeof(unsigned long long), st));
+    k_child_counts<<<grid_for(nseg, 256), 256, 0, st>>>(t.p.p, t.n.p, nseg, do_local,
+                                                        ws.child_cnt.p, nact_d.p);
+    CK_LAUNCH();
+    k_max_active_n<<<grid_for(nseg, 256), 256, 0, st>>>(t.p.p, t.n.p, nseg, do_local, maxn_d.p);
+    CK_LAUNCH();
+    int nact = 0;
+    unsigned long long maxn = 0;
+    d2h(&nact, nact_d.p, 1);
+    d2h(&maxn, maxn_d.p, 1);
+    sync();
+    if (level > 0) fill_seg_of_pos(t, ws.seg_of_pos.p, N);
+    if (nact == 0) break;
+    if (maxn <= (unsigned long long)SMALL_MAX) {
+      // every remaining level in the CTA-per-segment kernel, as the
+      // sort-per-level path does (it sorts each segment itself, so any order
+      // of a segment that is still cut will do; the others take their list)
+      k_ps_final<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ws.seg_of_pos.p, ws.oax.p,
+                                                    perm.p);
+      CK_LAUNCH();
+      const size_t smem = small_smem_bytes();
+      if (do_local) {
+        CK(cudaFuncSetAttribute(k_rcb_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        k_rcb_small<true><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
+            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
+      } else {
+        CK(cudaFuncSetAttribute(k_rcb_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+        k_rcb_small<false><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
+            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
+      }
+      CK_LAUNCH();
+      return;
+    }
+    ws.axis.ensure((size_t)nseg);
+    ws.split.ensure((size_t)nseg);
+    k_ps_axis<<<grid_for(nseg, 256), 256, 0, st>>>(ws.lists.p, ws.rank.p, ws.uniq.p, N, ndim,
+                                                   t.start.p, t.n.p, t.p.p, nseg, do_local,
+                                                   ws.axis.p, ws.split.p);
+    CK_LAUNCH();
+    k_ps_side<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ws.seg_of_pos.p, t.start.p,
+                                                ws.axis.p, ws.split.p, ws.side.p);
+    CK_LAUNCH();
+    k_ps_bsum<<<dim3((unsigned)nblk, (unsigned)ndim), PS_THREADS, 0, st>>>(
+        ws.lists.p, N, ws.seg_of_pos.p, ws.axis.p, ws.side.p, ws.bsum.p, nblk);
+    CK_LAUNCH();
+    k_ps_bscan<<<(unsigned)ndim, PS_THREADS, 0, st>>>(ws.bsum.p, nblk);
+    CK_LAUNCH();
+    k_ps_prefix<<<dim3((unsigned)nblk, (unsigned)ndim), PS_THREADS, 0, st>>>(
+        ws.lists.p, N, ws.seg_of_pos.p, ws.axis.p, ws.side.p, ws.bsum.p, nblk, ws.clg.p);
+    CK_LAUNCH();
+    k_ps_scatter<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ndim, ws.seg_of_pos.p,
+                                                   t.start.p, ws.axis.p, ws.split.p, ws.side.p,
+                                                   ws.clg.p, ws.lists2.p);
+    CK_LAUNCH();
+    std::swap(ws.lists.p, ws.lists2.p);
+    std::swap(ws.lists.n, ws.lists2.n);
+    // children, and the list that orders each of them
+    ws.child_off.ensure((size_t)nseg + 1);
+    const ll nchild = exclusive_scan_int_to_ll(ws.child_cnt.p, ws.child_off.p, nseg);
+    ws.t2.reserve(nchild);
+    k_children<<<grid_for(nseg, 256), 256, 0, st>>>(
+        t.start.p, t.n.p, t.p.p, t.r0.p, nseg, do_local, ws.child_off.p, ws.t2.start.p,
+        ws.t2.n.p, ws.t2.p.p, ws.t2.r0.p);
+    CK_LAUNCH();
+    ws.oax2.ensure((size_t)nchild);
+    k_ps_oaxis<<<grid_for(nseg, 256), 256, 0, st>>>(ws.axis.p, ws.oax.p, nseg, ws.child_off.p,
+                                                    ws.oax2.p);
+    CK_LAUNCH();
+    std::swap(ws.oax.p, ws.oax2.p);
+    std::swap(ws.oax.n, ws.oax2.n);
+    ws.t2.count = nchild;
+    std::swap(t.start, ws.t2.start);
+    std::swap(t.n, ws.t2.n);
+    std::swap(t.p, ws.t2.p);
+    std::swap(t.r0, ws.t2.r0);
+    std::swap(t.count, ws.t2.count);
+  }
+  k_ps_final<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ws.seg_of_pos.p, ws.oax.p, perm.p);
+  CK_LAUNCH();
+  if (part_of_elem) {
+    k_part_from_segs<<<grid_for(N, 256), 256, 0, st>>>(perm.p, ws.seg_of_pos.p, t.r0.p, N,
+                                                        part_of_elem);
+    CK_LAUNCH();
+  }
+}
+
 void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
                      const double *cent, ll N, int ndim, bool do_local,
                      int *part_of_elem, BisectWs &ws) {
@@ -1019,21 +1349,34 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
     // dense ranks of the centroid coordinates, once per set of centroids
     ws.rank.ensure((size_t)3 * N);
     ws.uniq.ensure((size_t)3 * N);
+    ws.sorted.ensure((size_t)ndim * N);
     DBuf<int> flag((size_t)N);
     DBuf<ll> excl((size_t)N);
+    ws.unique = true;
     for (int a = 0; a < ndim; a++) {
       k_axis_keys<<<grid_for(N, 256), 256, 0, st>>>(cent, N, a, ws.keys.p, ws.vals.p);
       CK_LAUNCH();
       seg_sort_pairs(ws.keys, ws.vals, N, nullptr, 1, ws.sort);
       k_rank_flags<<<grid_for(N, 256), 256, 0, st>>>(ws.keys.p, N, flag.p);
       CK_LAUNCH();
-      exclusive_scan_int_to_ll(flag.p, excl.p, N);
+      const ll changes = exclusive_scan_int_to_ll(flag.p, excl.p, N);
+      if (changes != N - 1) ws.unique = false;  // two centroids share a coordinate
       k_rank_write<<<grid_for(N, 256), 256, 0, st>>>(ws.keys.p, ws.vals.p, flag.p, excl.p, N,
                                                       ws.rank.p + (ll)a * N,
                                                       ws.uniq.p + (ll)a * N);
       CK_LAUNCH();
+      CK(cudaMemcpyAsync(ws.sorted.p + (ll)a * N, ws.vals.p, (size_t)N * sizeof(int),
+                         cudaMemcpyDeviceToDevice, st));
     }
     ws.rank_of = cent;
+  }
+  // PARRSB_GPU_RCB_PRESORT=0: the sort-per-level path even for unique ranks
+  if (kind == BISECT_RCB && ws.unique) {
+    const char *e = getenv("PARRSB_GPU_RCB_PRESORT");
+    if (!(e && atoi(e) == 0)) {
+      rcb_presorted(perm, t, N, ndim, do_local, part_of_elem, ws);
+      return;
+    }
   }
   for (int level = 0; level < 200; level++) {
     ll nseg = t.count;

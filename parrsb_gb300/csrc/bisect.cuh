@@ -40,6 +40,14 @@ struct BisectWs {
   DBuf<double> uniq;
   DBuf<u32> rbox;  // per segment: min rank (3), min complemented rank (3)
   const double *rank_of = nullptr;
+  // presorted-list RCB (every axis rank unique): the elements in rank order
+  // per axis (3 x N, with the ranks), the per-segment lists and their
+  // partition scratch
+  DBuf<int> sorted;
+  bool unique = false;
+  DBuf<int> lists, lists2, clg, oax, oax2, bsum;
+  DBuf<unsigned char> side;
+  DBuf<ll> split;
 };
 
 // Recursive bisection of every segment of `t` (segments tile [0, N) of the

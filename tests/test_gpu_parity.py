@@ -450,3 +450,39 @@ def test_timing_mode_same_partition(monkeypatch, graphs):
     st = P.last_stats()
     np.testing.assert_array_equal(a, b)
     assert st.spmv_ms > 0 and st.lanczos_ms[0] > 0 and st.lanczos_ms[1] > 0
+
+
+@pytest.mark.parametrize("case", ["box_seq", "box_part", "annulus_seq", "tagged", "rsb_pre"])
+def test_rcb_presorted_bitwise(oracle, monkeypatch, case):
+    """RCB on presorted coordinate lists (taken when no two centroids share a
+    coordinate on any axis) gives bitwise the parts and orders of the
+    sort-per-level path: one segment with and without the local recursion,
+    a 2D annulus, several tagged segments, and RSB's RCB pre-partition of
+    every group of every level."""
+    def run():
+        if case == "box_seq":
+            vtx, xyz = meshgen.box_hex(40, 36, 20, jitter=0.1, seed=31)
+            return P.part_mesh_seq(vtx, xyz, 77, partitioner=1)
+        if case == "box_part":
+            vtx, xyz = meshgen.box_hex(40, 36, 20, jitter=0.1, seed=32)
+            return (P.part_mesh(vtx, xyz, 1000, partitioner=1),)
+        if case == "annulus_seq":
+            vtx, xyz = meshgen.annulus_quad(256, 128, amp=0.02, seed=3)
+            return P.part_mesh_seq(vtx, xyz, 300, partitioner=1)
+        if case == "tagged":
+            vtx, xyz = meshgen.box_hex(30, 20, 16, jitter=0.1, seed=33)
+            tag = (np.arange(len(vtx)) * 7 % 5).astype(np.int32)
+            return (P.part_mesh(vtx, xyz, 40, partitioner=1, tagged=1, tag=tag),)
+        vtx, xyz = meshgen.box_hex(36, 30, 20, jitter=0.1, seed=34)
+        part = P.part_mesh(vtx, xyz, 64, partitioner=0)
+        st = P.last_stats()
+        return (part, np.array([st.lanczos_iters, st.max_fiedler_resid]))
+    a = run()
+    monkeypatch.setenv("PARRSB_GPU_RCB_PRESORT", "0")
+    b = run()
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    if case == "box_seq":  # and the oracle's
+        vtx, xyz = meshgen.box_hex(40, 36, 20, jitter=0.1, seed=31)
+        rc, ref, _, _, _ = oracle.part_mesh(vtx, xyz, 77, partitioner=1)
+        np.testing.assert_array_equal(a[0], ref)
