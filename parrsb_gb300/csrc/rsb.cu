@@ -81,11 +81,19 @@ __global__ void k_scatter_inv(const int *__restrict__ vals, ll n, int *__restric
 // its vertices, vertex by vertex, each run in slot order; an element b != a
 // occurs once per (vertex of a, equal vertex of b) pair, so its weight is its
 // number of occurrences, and the row lists every b at its first occurrence.
-// Up to GR_CAP candidates sit in shared memory; a longer list is read from
-// the runs again.  FILL = false: row lengths and the largest weight;
+// Up to GR_CAP candidates sit in shared memory, where a per-warp open-
+// addressing table (GR_HASH slots: element, count, first index) counts each
+// element's occurrences and keeps its first one in O(C) instead of
+// comparing every pair; a longer list is read from the runs again and
+// compared pairwise.  FILL = false: row lengths and the largest weight;
 // FILL = true: columns and weights at rowptr[a].
 constexpr int GR_WARPS = 4;
 constexpr int GR_CAP = 256;
+constexpr int GR_HASH = 512;  // power of two, twice GR_CAP: probe chains stay short
+
+__device__ __forceinline__ int gr_slot0(int b) {
+  return (int)(((unsigned)b * 2654435761u) >> 23);  // Fibonacci hashing to 9 bits
+}
 
 template <bool FILL>
 __global__ void __launch_bounds__(GR_WARPS * 32)
@@ -94,7 +102,11 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
              const ll *__restrict__ rowptr, int *__restrict__ col,
              unsigned char *__restrict__ wout, ll *__restrict__ rowlen, int *__restrict__ maxw) {
   __shared__ __align__(16) int cand[GR_WARPS][GR_CAP + 4];
+  __shared__ int hkey[GR_WARPS][GR_HASH], hcnt[GR_WARPS][GR_HASH], hfirst[GR_WARPS][GR_HASH];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int h = lane; h < GR_HASH; h += 32)  // empty: key -1, count 0, first INT_MAX
+    hkey[wid][h] = -1, hcnt[wid][h] = 0, hfirst[wid][h] = 0x7fffffff;
+  __syncwarp();
   const unsigned lt = (1u << lane) - 1u;
   const ll a = (ll)blockIdx.x * GR_WARPS + wid;
   int wmax = 0;
@@ -122,8 +134,20 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
       return sorted_slot[base + t] / nv;
     };
     const bool staged = C <= GR_CAP;
-    if (staged) {  // padded to a multiple of four with -2 (never an element)
-      for (ll t = lane; t < ((C + 3) & ~3ll); t += 32) cand[wid][t] = t < C ? cand_at(t) : -2;
+    if (staged) {
+      for (ll t = lane; t < C; t += 32) {
+        const int b = cand_at(t);
+        cand[wid][t] = b;
+        if (b == (int)a) continue;
+        int h = gr_slot0(b);
+        for (;;) {  // at most C distinct keys in GR_HASH > C slots: a free or equal slot exists
+          const int prev = atomicCAS(&hkey[wid][h], -1, b);
+          if (prev == -1 || prev == b) break;
+          h = (h + 1) & (GR_HASH - 1);
+        }
+        atomicAdd(&hcnt[wid][h], 1);
+        atomicMin(&hfirst[wid][h], (int)t);
+      }
       __syncwarp();
     }
     ll out = 0;
@@ -134,24 +158,20 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
       if (t < C) {
         b = staged ? cand[wid][t] : cand_at(t);
         if (b != (int)a) {
-          int before = 0;  // occurrences of b ahead of t
           if (staged) {
-            const int4 *c4 = reinterpret_cast<const int4 *>(cand[wid]);
-            for (int j = 0; j < (int)C; j += 4) {
-              const int4 v = c4[j >> 2];
-              const int m0 = v.x == b, m1 = v.y == b, m2 = v.z == b, m3 = v.w == b;
-              cnt += m0 + m1 + m2 + m3;
-              before += (m0 & (j < t)) + (m1 & (j + 1 < t)) + (m2 & (j + 2 < t)) +
-                        (m3 & (j + 3 < t));
-            }
+            int h = gr_slot0(b);
+            while (hkey[wid][h] != b) h = (h + 1) & (GR_HASH - 1);  // b was inserted
+            cnt = hcnt[wid][h];
+            first = hfirst[wid][h] == (int)t;
           } else {
+            int before = 0;  // occurrences of b ahead of t
             for (ll j = 0; j < C; j++) {
               const int m = cand_at(j) == b;
               cnt += m;
               before += m & (j < t);
             }
+            first = before == 0;
           }
-          first = before == 0;
         }
       }
       const unsigned m = __ballot_sync(0xffffffffu, first);
@@ -166,6 +186,28 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
       out += __popc(m);
     }
     if (!FILL && lane == 0) rowlen[a] = out;
+    if (staged) {  // empty the table again: find every used slot, then clear
+      __syncwarp();
+      int hs[GR_CAP / 32];
+#pragma unroll
+      for (int k = 0; k < GR_CAP / 32; k++) {
+        const ll t = lane + 32 * k;
+        hs[k] = -1;
+        if (t < C) {
+          const int b = cand[wid][t];
+          if (b != (int)a) {
+            int h = gr_slot0(b);
+            while (hkey[wid][h] != b) h = (h + 1) & (GR_HASH - 1);
+            hs[k] = h;
+          }
+        }
+      }
+      __syncwarp();
+#pragma unroll
+      for (int k = 0; k < GR_CAP / 32; k++)
+        if (hs[k] >= 0) hkey[wid][hs[k]] = -1, hcnt[wid][hs[k]] = 0, hfirst[wid][hs[k]] = 0x7fffffff;
+      __syncwarp();
+    }
   }
   if (!FILL) {  // one atomic per warp; every lane reaches the shuffles
     for (int off = 16; off > 0; off >>= 1)
