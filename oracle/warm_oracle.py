@@ -73,9 +73,11 @@ def spacings(cent, group, rows, cols, w, wface=4):
 
 def frames(cent, group, rows, cols, w):
     """Per group: mean, principal axes (rows, largest variance first, largest
-    component positive; axes within 5% take the first inside their plane
-    along the coordinate axis of largest variance) and 1 / sqrt(3 l1 / n),
-    all of the centroids measured in element spacings (spacings())."""
+    component positive) and 1 / sqrt(3 l1 / n), all of the centroids
+    measured in element spacings (spacings()).  When the two largest
+    variances are within 5% the axes are the coordinate axes with RCB's cut
+    axis first (longest edge of the raw centroids' bounding box, ties to the
+    lower axis) and l1 is the scatter along it."""
     out = {}
     sp = spacings(cent, group, rows, cols, w)
     for g in np.unique(group[group >= 0]):
@@ -88,11 +90,15 @@ def frames(cent, group, rows, cols, w):
         o = np.argsort(-lam, kind="stable")
         lam, R = lam[o], V[:, o].T.copy()
         if lam[0] > 0 and lam[0] - lam[1] <= 0.05 * lam[0]:
-            ax = int(np.argmax(np.diag(A)))
-            u = R[0, ax] * R[0] + R[1, ax] * R[1]
-            if np.linalg.norm(u) > 1e-6:
-                R[0] = u / np.linalg.norm(u)
-                R[1] = np.cross(R[2], R[0])
+            raw = cent[group == g]
+            ext = raw.max(axis=0) - raw.min(axis=0)
+            ax = 0  # (a 2D mesh has ext[2] = 0, which is never strictly longer)
+            for a in range(1, 3):
+                if ext[a] > ext[ax]:
+                    ax = a
+            R = np.eye(3)[[ax] + [a for a in range(3) if a != ax]]
+            lam = lam.copy()
+            lam[0] = A[ax, ax]
         for a in range(3):
             if R[a, np.argmax(np.abs(R[a]))] < 0:
                 R[a] = -R[a]

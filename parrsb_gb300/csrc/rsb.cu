@@ -2261,9 +2261,9 @@ struct Lanczos {
       tried++;
       lf += log10(std::max(r_fb[g], 1e-300));
       lw += log10(std::max(rw, 1e-300));
-      // a group with two axes of nearly the same length keeps the fallback
-      const bool dg = g < (int)degen.size() && degen[g];
-      use[g] = (!dg && rw < r_fb[g]) ? 1 : 0;  // NaN never wins
+      // (a group with two axes of nearly the same length has its guess
+      // along RCB's cut axis, the axis of the fallback's step)
+      use[g] = rw < r_fb[g] ? 1 : 0;  // NaN never wins
       S.warm_used += use[g];
     }
     // running geometric means over every judged group of the call

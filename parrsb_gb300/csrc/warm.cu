@@ -223,29 +223,50 @@ __global__ void k_mp_scales(const double *__restrict__ part, const int *__restri
 
 // per tile: sum of (c - o), sum of (c - o)(c - o)^T (6) about the group's
 // origin o = centroid of its first position (numerically safe raw moments),
-// coordinates in element spacings
+// coordinates in element spacings; and the tile's bounding box of the raw
+// centroids (min x y z, max x y z), from which RCB picks its cut axis
 __global__ void __launch_bounds__(256)
 k_mp_moments(const FTile *__restrict__ tiles, const ll *__restrict__ gstart,
              const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
-             const double *__restrict__ sa, double *__restrict__ part) {
+             const double *__restrict__ sa, double *__restrict__ part,
+             double *__restrict__ box) {
   const FTile t = tiles[blockIdx.x];
   const int e0 = perm[gstart[t.g]];
   const double o[3] = {cent[e0], cent[nel + e0], cent[2 * nel + e0]};
   const double *k = sa + (ll)t.g * 3;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double lo[3] = {o[0], o[1], o[2]}, hi[3] = {o[0], o[1], o[2]};
   for (ll i = t.b + threadIdx.x; i < t.e; i += blockDim.x) {
     const int e = perm[i];
-    const double x = (cent[e] - o[0]) * k[0], y = (cent[nel + e] - o[1]) * k[1],
-                 z = (cent[2 * nel + e] - o[2]) * k[2];
+    const double c[3] = {cent[e], cent[nel + e], cent[2 * nel + e]};
+    const double x = (c[0] - o[0]) * k[0], y = (c[1] - o[1]) * k[1], z = (c[2] - o[2]) * k[2];
     s[0] += x, s[1] += y, s[2] += z;
     s[3] += x * x, s[4] += y * y, s[5] += z * z;
     s[6] += x * y, s[7] += x * z, s[8] += y * z;
+    for (int a = 0; a < 3; a++) lo[a] = fmin(lo[a], c[a]), hi[a] = fmax(hi[a], c[a]);
   }
   __shared__ double sh[32];
   for (int q = 0; q < 9; q++) {
     const double v = mp_block_sum(s[q], sh);
     if (threadIdx.x == 0) part[(ll)blockIdx.x * 9 + q] = v;
     __syncthreads();
+  }
+  // the box: o lies in the group, so starting from it leaves min / max exact
+  __shared__ double bx[6][8];
+  for (int a = 0; a < 3; a++) {
+    for (int off = 16; off > 0; off >>= 1) {
+      lo[a] = fmin(lo[a], __shfl_down_sync(0xffffffffu, lo[a], off));
+      hi[a] = fmax(hi[a], __shfl_down_sync(0xffffffffu, hi[a], off));
+    }
+  }
+  if ((threadIdx.x & 31) == 0)
+    for (int a = 0; a < 3; a++) bx[a][threadIdx.x >> 5] = lo[a], bx[3 + a][threadIdx.x >> 5] = hi[a];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = bx[threadIdx.x][0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+      v = threadIdx.x < 3 ? fmin(v, bx[threadIdx.x][w]) : fmax(v, bx[threadIdx.x][w]);
+    box[(ll)blockIdx.x * 6 + threadIdx.x] = v;
   }
 }
 
@@ -289,9 +310,12 @@ __device__ void jacobi3(double A[3][3], double d[3], double V[3][3]) {
 // One thread per group: mean, scatter matrix, principal axes (largest
 // variance first; each axis signed so that its largest component is
 // positive), scale.  When the two largest variances are within 5% the
-// first axis is taken inside their plane along the coordinate axis of
-// largest variance (the axis RCB would cut), so that a nearly degenerate
-// group gets the cut direction the reference's own start vector favours.
+// frame is the coordinate axes with RCB's cut axis first (the longest edge
+// of the raw centroids' bounding box, ties to the lower axis) and the scale
+// of the variance along it: the reference's step start separates the two
+// halves of exactly that axis, and a guess along the same coordinate axis
+// excites the same modes of a nearly degenerate pair (any other direction
+// in their plane would excite both).  degen[g] = 1 for such a group.
 // frame[g] = {mu[3], R[3][3] (rows = axes), 1/s, sa[3]}: mu in element
 // spacings, x~ = R (c * sa - mu) / s.
 __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__restrict__ part,
@@ -299,7 +323,8 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
                             const ll *__restrict__ gstart, const ll *__restrict__ gn,
                             const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
                             int ngroups, int ndim, const double *__restrict__ sa,
-                            double *__restrict__ frame, int *__restrict__ degen) {
+                            const double *__restrict__ box, double *__restrict__ frame,
+                            int *__restrict__ degen) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngroups) return;
   double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -333,22 +358,24 @@ __global__ void k_mp_frames(const FTile *__restrict__ tiles, const double *__res
   double R[3][3];
   for (int a = 0; a < 3; a++)
     for (int k = 0; k < 3; k++) R[a][k] = V[k][ord[a]];
-  const double l1 = d[ord[0]], l2 = d[ord[1]];
-  degen[g] = (l1 > 0.0 && (l1 - l2) <= 0.05 * l1) ? 1 : 0;
-  if (l1 > 0.0 && (l1 - l2) <= 0.05 * l1) {
-    int ax = 0;  // coordinate axis of largest variance (first strict maximum)
-    for (int k = 1; k < 3; k++)
-      if (A[k][k] > A[ax][ax]) ax = k;
-    double u[3];  // projection of e_ax on span(R0, R1)
-    for (int k = 0; k < 3; k++) u[k] = R[0][ax] * R[0][k] + R[1][ax] * R[1][k];
-    const double un = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
-    if (un > 1e-6) {
-      for (int k = 0; k < 3; k++) R[0][k] = u[k] / un;
-      // R1 = R2 x R0 keeps the frame orthonormal
-      R[1][0] = R[2][1] * R[0][2] - R[2][2] * R[0][1];
-      R[1][1] = R[2][2] * R[0][0] - R[2][0] * R[0][2];
-      R[1][2] = R[2][0] * R[0][1] - R[2][1] * R[0][0];
+  double l1 = d[ord[0]];
+  const double l2 = d[ord[1]];
+  const bool dg = l1 > 0.0 && (l1 - l2) <= 0.05 * l1;
+  degen[g] = dg ? 1 : 0;
+  if (dg) {
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; a++) lo[a] = box[(ll)tile0[g] * 6 + a], hi[a] = box[(ll)tile0[g] * 6 + 3 + a];
+    for (int t = tile0[g] + 1; t < tile0[g] + ntile[g]; t++)
+      for (int a = 0; a < 3; a++)
+        lo[a] = fmin(lo[a], box[(ll)t * 6 + a]), hi[a] = fmax(hi[a], box[(ll)t * 6 + 3 + a]);
+    int ax = 0;  // RCB's rule: strictly longer wins
+    for (int a = 1; a < ndim; a++)
+      if (hi[a] - lo[a] > hi[ax] - lo[ax]) ax = a;
+    for (int a = 0, r = 1; a < 3; a++) {
+      for (int q = 0; q < 3; q++) R[a == ax ? 0 : r][q] = a == q ? 1.0 : 0.0;
+      if (a != ax) r++;
     }
+    l1 = A[ax][ax];
   }
   for (int a = 0; a < 3; a++) {
     int big = 0;
@@ -1032,7 +1059,7 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     h2d(dn.p, nt.data(), G);
     h2d(gs.p, v.gstart.data(), G);
     h2d(gn.p, v.gn.data(), G);
-    DBuf<double> part(tiles.size() * 9);
+    DBuf<double> part(tiles.size() * 9), box(tiles.size() * 6);
     const unsigned wface = ndim == 3 ? 4u : 2u;  // face (3D) or edge (2D) neighbours
     if (esp)
       k_mp_spacing_elem<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, v.perm, esp, part.p);
@@ -1044,10 +1071,11 @@ void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<doubl
     k_mp_scales<<<grid_for(G, 128), 128, 0, st>>>(part.p, d0.p, dn.p, G, sa.p);
     CK_LAUNCH();
     k_mp_moments<<<(unsigned)tiles.size(), 256, 0, st>>>(dt.p, gs.p, v.perm, cent, nel, sa.p,
-                                                        part.p);
+                                                        part.p, box.p);
     CK_LAUNCH();
     k_mp_frames<<<grid_for(G, 128), 128, 0, st>>>(dt.p, part.p, d0.p, dn.p, gs.p, gn.p, v.perm,
-                                                  cent, nel, G, ndim, sa.p, frame.p, dg.p);
+                                                  cent, nel, G, ndim, sa.p, box.p, frame.p,
+                                                  dg.p);
     CK_LAUNCH();
   }
   if (degen) {
