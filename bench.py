@@ -638,7 +638,7 @@ def main():
                    "start": ("geometric warm start -sin(pi x1/2) along each group's principal "
                              "axis in element spacings, judged per group against the "
                              "reference's step start by FP64 eigen-residual; groups with two "
-                             "axes within 5% keep the step start"
+                             "axes within 5% take it along RCB's cut axis"
                              if args.method == "warm" else
                              "learned warm start (network), judged per group the same way"
                              if args.method == "learned" else "the reference's step start"),

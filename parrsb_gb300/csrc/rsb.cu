@@ -2232,11 +2232,9 @@ struct Lanczos {
   // Start vectors with a predicted candidate y (FP64 per position): every
   // group starts from y or from the fallback start (start_kind 1: random,
   // otherwise the reference's step vector), whichever has the lower FP64
-  // eigen-residual ||L f - rho f|| / ||f|| (the judge); groups flagged in
-  // degen (two nearly equal principal axes) keep the fallback.  Leaves the
-  // start in f.
-  void choose_start(const Level &lv, const double *y, int start_kind,
-                    const std::vector<int> &degen) {
+  // eigen-residual ||L f - rho f|| / ||f|| (the judge).  Leaves the start
+  // in f.
+  void choose_start(const Level &lv, const double *y, int start_kind) {
     cudaStream_t st = ctx().stream;
     k_set_active<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
     CK_LAUNCH();
@@ -3142,7 +3140,7 @@ template <typename VT>
 void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
                        const std::vector<ll> &gstart, const std::vector<ll> &gn, ll N,
                        double *f_pos, std::vector<GState> &res,
-                       const double *y_warm = nullptr, const std::vector<int> &degen = {}) {
+                       const double *y_warm = nullptr) {
   lz.setup(gstart, gn, N, o.miter);
   lz.reorth = o.reorth != 0;
   if (lz.reorth) {
@@ -3154,7 +3152,7 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
   {
     StageTimer tm(PARRSB_STAGE_LANCZOS);
     const auto h0 = std::chrono::steady_clock::now();
-    if (y_warm) lz.choose_start(lv, y_warm, o.start, degen);
+    if (y_warm) lz.choose_start(lv, y_warm, o.start);
     ctx().stats.lanczos_host_ms[0] +=
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
     lz.run(lv, o.tol, o.mpass, o.use_graphs != 0, y_warm != nullptr, o.start);
@@ -3329,7 +3327,6 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     // (the network where groups have at least warm_min elements; with
     // start 2 the geometric guess elsewhere)
     const double *y_warm = nullptr;
-    std::vector<int> degen;
     if ((o.warm || o.start == 2) && nv == 8) {
       ll biggest = 0;
       for (int g = 0; g < na; g++) biggest = std::max(biggest, an[g]);
@@ -3347,11 +3344,11 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
           element_spacings(G, cent, N, ndim, esp.p);
         }
         if (use_net)
-          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p, &degen,
+          warm_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p, nullptr,
                              esp.p);
         else  // start 2: the geometric guess
           geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p,
-                                  &degen, esp.p);
+                                  nullptr, esp.p);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;
@@ -3365,7 +3362,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
     // ---- Fiedler vectors (src/rsb.c:300-302)
     std::vector<GState> res;
     if (o.batched) {
-      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res, y_warm, degen);
+      run_fiedler_level<VT>(lz, lv, o, ast, an, N, f_pos.p, res, y_warm);
     } else {
       // plain path: every group of the level solved by its own launches
       RsbOpts o1 = o;
@@ -3373,8 +3370,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
       for (int g = 0; g < na; g++) {
         std::vector<GState> r1;
         std::vector<ll> s1 = {ast[g]}, n1 = {an[g]};
-        std::vector<int> d1 = {g < (int)degen.size() ? degen[g] : 0};
-        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1, y_warm, d1);
+        run_fiedler_level<VT>(lz, lv, o1, s1, n1, N, f_tmp.p, r1, y_warm);
         CK(cudaMemcpyAsync(f_pos.p + ast[g], f_tmp.p + ast[g], an[g] * sizeof(double),
                            cudaMemcpyDeviceToDevice, st));
         res.push_back(r1[0]);

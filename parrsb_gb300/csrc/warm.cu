@@ -1034,7 +1034,8 @@ void mp_features(const MpView &v, const double *cent, ll nel, int ndim, MpBuffer
 }
 
 // Per group: {mu[3], R[3][3], 1/s} (k_mp_frames); degen (optional): per
-// group, 1 when its two largest centroid variances are within 5%.
+// group, 1 when its two largest centroid variances are within 5% (its frame
+// is then RCB's cut axis first).
 void mp_frames(const MpView &v, const double *cent, ll nel, int ndim, DBuf<double> &frame,
                std::vector<int> *degen, const float4 *esp) {
   cudaStream_t st = ctx().stream;
