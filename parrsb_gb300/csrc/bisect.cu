@@ -1193,6 +1193,229 @@ __global__ void k_ps_final(const int *__restrict__ lists, ll N, const int *__res
   if (a >= 0) perm[j] = lists[(ll)a * N + j];
 }
 
+// The remaining levels of every segment of at most SMALL_MAX elements in
+// one CTA each, on presorted lists (every rank unique).  An element's local
+// id is its place in the segment's axis-0 list at launch; the CTA holds the
+// segment's three lists of local ids in shared memory and, per level, for
+// every active sub-range (tracked per position in registers as k_rcb_small
+// does): its cut axis from the first and last entry of each list, the side
+// of each element from the cut axis' list, and a stable partition of every
+// list by side (a CTA-wide prefix count).  Same tree, same order as the
+// sort-per-level kernels; without LOCAL a sub-range that is no longer cut
+// keeps the list of the axis that cut it last.
+constexpr size_t pss_smem_bytes() {  // 4 lists + prefix counts (u16), side + axis (u8)
+  return (size_t)SMALL_MAX * (5 * sizeof(unsigned short) + 2);
+}
+
+__device__ __forceinline__ int pss_excl_scan(int v, int *wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int s = wsum[lane];  // SMALL_WARPS == 32
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    wsum[lane] = s;
+  }
+  __syncthreads();
+  const int r = (warp ? wsum[warp - 1] : 0) + x - v;
+  __syncthreads();
+  return r;
+}
+
+template <bool LOCAL>
+__global__ void __launch_bounds__(SMALL_THREADS)
+k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__restrict__ loc,
+               const u32 *__restrict__ rank, const double *__restrict__ uniq, ll N, int ndim,
+               const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
+               const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
+               int *__restrict__ part) {
+  extern __shared__ __align__(16) unsigned char pss_smem[];
+  unsigned short *buf = reinterpret_cast<unsigned short *>(pss_smem);  // 4 list buffers
+  unsigned short *cl = buf + 4 * SMALL_MAX;                             // prefix counts
+  unsigned char *side = reinterpret_cast<unsigned char *>(cl + SMALL_MAX);
+  unsigned char *sax = side + SMALL_MAX;  // cut axis by sub-range start
+  __shared__ int wsum[SMALL_WARPS];
+  __shared__ int lb[4];  // buffer of each list (lb[3]: the spare)
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ll sg = blockIdx.x;
+  const ll start = seg_start[sg];
+  const int n = (int)seg_n[sg], p0 = seg_p[sg], r0 = seg_r0[sg];
+  if (n <= 0 || p0 <= 0) return;
+  const bool seg_act = p0 > 1 || (LOCAL && p0 == 1 && n >= 2);
+  if (!seg_act || n > SMALL_MAX) {
+    if (part && n <= SMALL_MAX && p0 == 1)
+      for (int x = threadIdx.x; x < n; x += blockDim.x) part[perm[start + x]] = r0;
+    return;
+  }
+  const int *gl0 = lists + start;  // local id k -> element gl0[k]
+  for (int x = threadIdx.x; x < n; x += blockDim.x) loc[gl0[x]] = x;
+  __syncthreads();
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    buf[x] = (unsigned short)x;
+    for (int d = 1; d < ndim; d++)
+      buf[d * SMALL_MAX + x] = (unsigned short)loc[lists[(ll)d * N + start + x]];
+  }
+  if (threadIdx.x < 4) lb[threadIdx.x] = threadIdx.x < ndim ? threadIdx.x : 3;
+  // sub-range of each own position (start | length << 16), its virtual
+  // ranks, and the axis that cut it last
+  u32 sl_r[SMALL_ITEMS];
+  int p_r[SMALL_ITEMS];
+  signed char oax_r[SMALL_ITEMS];
+#pragma unroll
+  for (int r = 0; r < SMALL_ITEMS; r++) sl_r[r] = (u32)n << 16, p_r[r] = p0, oax_r[r] = -1;
+  __syncthreads();
+  for (int d = 0; d < 64; d++) {
+    if (d > 0) {  // advance every position's sub-range by the previous cut
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
+        int L, h;
+        if (p > 1) {
+          L = lower_count_small(ln, p);
+          h = (p + 1) / 2;
+        } else if (LOCAL && ln >= 2) {
+          L = ln / 2;
+          h = 0;
+        } else {
+          continue;
+        }
+        oax_r[r] = (signed char)sax[st];
+        if (x < st + L) {
+          ln = L;
+          p = p > 1 ? h : p;
+        } else {
+          st += L;
+          ln -= L;
+          p = p > 1 ? p - h : p;
+        }
+        sl_r[r] = (u32)st | ((u32)ln << 16);
+        p_r[r] = p;
+      }
+    }
+    __syncthreads();  // every sax read above is done
+    u32 act = 0;
+#pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
+      const int ln = (int)(sl_r[r] >> 16);
+      if (x < n && (p_r[r] > 1 || (LOCAL && ln >= 2))) act |= 1u << r;
+    }
+    if (!__syncthreads_or(act != 0)) break;
+    // cut axis of each active sub-range: the ranks of the first and last
+    // entry of each list
+#pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
+      const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16);
+      if (!((act >> r) & 1u) || x != st) continue;
+      double len[3] = {0.0, 0.0, 0.0};
+      for (int q = 0; q < ndim; q++) {
+        const unsigned short *Lq = buf + lb[q] * SMALL_MAX;
+        const u32 lo = rank[(ll)q * N + gl0[Lq[st]]], hi = rank[(ll)q * N + gl0[Lq[st + ln - 1]]];
+        len[q] = __dsub_rn(uniq[(ll)q * N + hi], uniq[(ll)q * N + lo]);
+      }
+      int ax = 0;
+      for (int q = 1; q < ndim; q++)
+        if (len[q] > len[ax]) ax = q;
+      sax[st] = (unsigned char)ax;
+    }
+    __syncthreads();
+    // side of every element of a cut sub-range, from the cut axis' list
+#pragma unroll
+    for (int r = 0; r < SMALL_ITEMS; r++) {
+      if (!((act >> r) & 1u)) continue;
+      const int x = warp * SMALL_SPAN + r * 32 + lane;
+      const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
+      const int L = p > 1 ? lower_count_small(ln, p) : ln / 2;
+      side[buf[lb[sax[st]] * SMALL_MAX + x]] = (x - st) >= L ? 1 : 0;
+    }
+    __syncthreads();
+    // stable partition of each list by side, into the spare buffer
+    for (int q = 0; q < ndim; q++) {
+      const unsigned short *Lq = buf + lb[q] * SMALL_MAX;
+      unsigned short *Tq = buf + lb[3] * SMALL_MAX;
+      // lower flag by position (written by the thread that tracks the
+      // position's sub-range, read back in contiguous runs for the scan)
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        if (x >= n) continue;
+        const bool a = (act >> r) & 1u;
+        cl[x] = (unsigned short)(a ? (side[Lq[x]] == 0 ? 1 : 0) : 1);
+      }
+      __syncthreads();
+      int v[SMALL_ITEMS], c = 0;
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = threadIdx.x * SMALL_ITEMS + r;
+        v[r] = x < n ? (int)cl[x] : 0;
+        c += v[r];
+      }
+      int run = pss_excl_scan(c, wsum);
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = threadIdx.x * SMALL_ITEMS + r;
+        if (x < n) cl[x] = (unsigned short)run;  // lower flags before x (x < 8192)
+        run += v[r];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        if (x >= n) continue;
+        int dest = x;
+        const unsigned short id = Lq[x];
+        if ((act >> r) & 1u) {
+          const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
+          const int L = p > 1 ? lower_count_small(ln, p) : ln / 2;
+          const int before = (int)cl[x] - (int)cl[st];
+          dest = side[id] == 0 ? st + before : st + L + (x - st - before);
+        }
+        Tq[dest] = id;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const int t2 = lb[3];
+        lb[3] = lb[q];
+        lb[q] = t2;
+      }
+      __syncthreads();
+    }
+  }
+  // order: a LOCAL recursion ends in single elements (every list agrees);
+  // otherwise each position takes the list of the axis that cut it last
+  int ev[SMALL_ITEMS];
+#pragma unroll
+  for (int r = 0; r < SMALL_ITEMS; r++) {
+    const int x = warp * SMALL_SPAN + r * 32 + lane;
+    ev[r] = 0;
+    if (x < n) {
+      const int a = oax_r[r] < 0 ? 0 : oax_r[r];
+      ev[r] = gl0[buf[lb[a] * SMALL_MAX + x]];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < SMALL_ITEMS; r++) {
+    const int x = warp * SMALL_SPAN + r * 32 + lane;
+    if (x < n) {
+      perm[start + x] = ev[r];
+      if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+    }
+  }
+}
+
 static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_local,
                           int *part_of_elem, BisectWs &ws) {
   cudaStream_t st = ctx().stream;
@@ -1244,25 +1467,23 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_
     if (level > 0) fill_seg_of_pos(t, ws.seg_of_pos.p, N);
     if (nact == 0) break;
     if (maxn <= (unsigned long long)SMALL_MAX) {
-      // every remaining level in the CTA-per-segment kernel, as the
-      // sort-per-level path does (it sorts each segment itself, so any order
-      // of a segment that is still cut will do; the others take their list)
+      // every remaining level in one CTA per segment, on the segment's lists
+      // (k_rcb_small_ps); a segment that is no longer cut takes its list here
       k_ps_final<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ws.seg_of_pos.p, ws.oax.p,
                                                     perm.p);
       CK_LAUNCH();
-      const size_t smem = small_smem_bytes();
+      ws.loc.ensure((size_t)N);
+      const size_t smem = pss_smem_bytes();
       if (do_local) {
-        CK(cudaFuncSetAttribute(k_rcb_small<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-        k_rcb_small<true><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
-            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
-            part_of_elem);
+        ensure_smem_limit(k_rcb_small_ps<true>, (int)smem);
+        k_rcb_small_ps<true><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
+            perm.p, ws.lists.p, ws.loc.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p,
+            t.r0.p, part_of_elem);
       } else {
-        CK(cudaFuncSetAttribute(k_rcb_small<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-        k_rcb_small<false><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
-            perm.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
-            part_of_elem);
+        ensure_smem_limit(k_rcb_small_ps<false>, (int)smem);
+        k_rcb_small_ps<false><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
+            perm.p, ws.lists.p, ws.loc.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p,
+            t.r0.p, part_of_elem);
       }
       CK_LAUNCH();
       return;

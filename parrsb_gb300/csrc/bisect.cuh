@@ -45,7 +45,7 @@ struct BisectWs {
   // partition scratch
   DBuf<int> sorted;
   bool unique = false;
-  DBuf<int> lists, lists2, clg, oax, oax2, bsum;
+  DBuf<int> lists, lists2, clg, oax, oax2, bsum, loc;
   DBuf<unsigned char> side;
   DBuf<ll> split;
 };
