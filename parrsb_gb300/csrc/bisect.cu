@@ -1203,8 +1203,8 @@ __global__ void k_ps_final(const int *__restrict__ lists, ll N, const int *__res
 // list by side (a CTA-wide prefix count).  Same tree, same order as the
 // sort-per-level kernels; without LOCAL a sub-range that is no longer cut
 // keeps the list of the axis that cut it last.
-constexpr size_t pss_smem_bytes() {  // 4 lists + prefix counts (u16), side + axis (u8)
-  return (size_t)SMALL_MAX * (5 * sizeof(unsigned short) + 2);
+constexpr size_t pss_smem_bytes() {  // 4 lists, prefix counts, splits (u16); side, axis (u8)
+  return (size_t)SMALL_MAX * (6 * sizeof(unsigned short) + 2);
 }
 
 __device__ __forceinline__ int pss_excl_scan(int v, int *wsum) {
@@ -1232,64 +1232,36 @@ __device__ __forceinline__ int pss_excl_scan(int v, int *wsum) {
   return r;
 }
 
-template <bool LOCAL>
-__global__ void __launch_bounds__(SMALL_THREADS)
-k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__restrict__ loc,
-               const u32 *__restrict__ rank, const double *__restrict__ uniq, ll N, int ndim,
-               const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
-               const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
-               int *__restrict__ part) {
-  extern __shared__ __align__(16) unsigned char pss_smem[];
-  unsigned short *buf = reinterpret_cast<unsigned short *>(pss_smem);  // 4 list buffers
-  unsigned short *cl = buf + 4 * SMALL_MAX;                             // prefix counts
-  unsigned char *side = reinterpret_cast<unsigned char *>(cl + SMALL_MAX);
-  unsigned char *sax = side + SMALL_MAX;  // cut axis by sub-range start
-  __shared__ int wsum[SMALL_WARPS];
-  __shared__ int lb[4];  // buffer of each list (lb[3]: the spare)
+// The level loop of k_rcb_small_ps; PONE: the segment has one virtual rank
+// (only the local halving: no rank counts to track, every part is r0).
+template <bool LOCAL, bool PONE>
+__device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__restrict__ gl0,
+                                           const u32 *__restrict__ rank,
+                                           const double *__restrict__ uniq, ll N, int ndim,
+                                           ll start, int n, int p0, int r0,
+                                           int *__restrict__ part, unsigned short *buf,
+                                           unsigned short *cl, unsigned short *spl,
+                                           unsigned char *side, unsigned char *sax, int *wsum,
+                                           int *lb) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const ll sg = blockIdx.x;
-  const ll start = seg_start[sg];
-  const int n = (int)seg_n[sg], p0 = seg_p[sg], r0 = seg_r0[sg];
-  if (n <= 0 || p0 <= 0) return;
-  const bool seg_act = p0 > 1 || (LOCAL && p0 == 1 && n >= 2);
-  if (!seg_act || n > SMALL_MAX) {
-    if (part && n <= SMALL_MAX && p0 == 1)
-      for (int x = threadIdx.x; x < n; x += blockDim.x) part[perm[start + x]] = r0;
-    return;
-  }
-  const int *gl0 = lists + start;  // local id k -> element gl0[k]
-  for (int x = threadIdx.x; x < n; x += blockDim.x) loc[gl0[x]] = x;
-  __syncthreads();
-  for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    buf[x] = (unsigned short)x;
-    for (int d = 1; d < ndim; d++)
-      buf[d * SMALL_MAX + x] = (unsigned short)loc[lists[(ll)d * N + start + x]];
-  }
-  if (threadIdx.x < 4) lb[threadIdx.x] = threadIdx.x < ndim ? threadIdx.x : 3;
   // sub-range of each own position (start | length << 16), its virtual
   // ranks, and the axis that cut it last
   u32 sl_r[SMALL_ITEMS];
-  int p_r[SMALL_ITEMS];
+  int p_r[PONE ? 1 : SMALL_ITEMS], rk_r[PONE ? 1 : SMALL_ITEMS];  // virtual ranks, first rank
   signed char oax_r[SMALL_ITEMS];
 #pragma unroll
-  for (int r = 0; r < SMALL_ITEMS; r++) sl_r[r] = (u32)n << 16, p_r[r] = p0, oax_r[r] = -1;
-  __syncthreads();
+  for (int r = 0; r < SMALL_ITEMS; r++) {
+    sl_r[r] = (u32)n << 16, oax_r[r] = -1;
+    if (!PONE) p_r[r] = p0, rk_r[r] = 0;
+  }
   for (int d = 0; d < 64; d++) {
     if (d > 0) {  // advance every position's sub-range by the previous cut
 #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
         const int x = warp * SMALL_SPAN + r * 32 + lane;
-        int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
-        int L, h;
-        if (p > 1) {
-          L = lower_count_small(ln, p);
-          h = (p + 1) / 2;
-        } else if (LOCAL && ln >= 2) {
-          L = ln / 2;
-          h = 0;
-        } else {
-          continue;
-        }
+        int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = PONE ? 1 : p_r[r];
+        if (!(p > 1 || (LOCAL && ln >= 2))) continue;  // no longer cut
+        const int L = spl[st], h = p > 1 ? (p + 1) / 2 : 0;
         oax_r[r] = (signed char)sax[st];
         if (x < st + L) {
           ln = L;
@@ -1298,9 +1270,10 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
           st += L;
           ln -= L;
           p = p > 1 ? p - h : p;
+          if (!PONE) rk_r[r] += h;
         }
         sl_r[r] = (u32)st | ((u32)ln << 16);
-        p_r[r] = p;
+        if (!PONE) p_r[r] = p;
       }
     }
     __syncthreads();  // every sax read above is done
@@ -1309,7 +1282,7 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
     for (int r = 0; r < SMALL_ITEMS; r++) {
       const int x = warp * SMALL_SPAN + r * 32 + lane;
       const int ln = (int)(sl_r[r] >> 16);
-      if (x < n && (p_r[r] > 1 || (LOCAL && ln >= 2))) act |= 1u << r;
+      if (x < n && ((!PONE && p_r[r] > 1) || (LOCAL && ln >= 2))) act |= 1u << r;
     }
     if (!__syncthreads_or(act != 0)) break;
     // cut axis of each active sub-range: the ranks of the first and last
@@ -1329,6 +1302,8 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
       for (int q = 1; q < ndim; q++)
         if (len[q] > len[ax]) ax = q;
       sax[st] = (unsigned char)ax;
+      const int p = PONE ? 1 : p_r[r];
+      spl[st] = (unsigned short)(p > 1 ? lower_count_small(ln, p) : ln / 2);
     }
     __syncthreads();
     // side of every element of a cut sub-range, from the cut axis' list
@@ -1336,9 +1311,8 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
     for (int r = 0; r < SMALL_ITEMS; r++) {
       if (!((act >> r) & 1u)) continue;
       const int x = warp * SMALL_SPAN + r * 32 + lane;
-      const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
-      const int L = p > 1 ? lower_count_small(ln, p) : ln / 2;
-      side[buf[lb[sax[st]] * SMALL_MAX + x]] = (x - st) >= L ? 1 : 0;
+      const int st = (int)(sl_r[r] & 0xFFFFu);
+      side[buf[lb[sax[st]] * SMALL_MAX + x]] = (x - st) >= (int)spl[st] ? 1 : 0;
     }
     __syncthreads();
     // stable partition of each list by side, into the spare buffer
@@ -1377,8 +1351,7 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
         int dest = x;
         const unsigned short id = Lq[x];
         if ((act >> r) & 1u) {
-          const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = p_r[r];
-          const int L = p > 1 ? lower_count_small(ln, p) : ln / 2;
+          const int st = (int)(sl_r[r] & 0xFFFFu), L = spl[st];
           const int before = (int)cl[x] - (int)cl[st];
           dest = side[id] == 0 ? st + before : st + L + (x - st - before);
         }
@@ -1411,9 +1384,52 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
     const int x = warp * SMALL_SPAN + r * 32 + lane;
     if (x < n) {
       perm[start + x] = ev[r];
-      if (part) part[ev[r]] = r0 + descend<LOCAL>(x, n, p0, 64).rank;
+      if (part) part[ev[r]] = r0 + (PONE ? 0 : rk_r[r]);
     }
   }
+}
+
+template <bool LOCAL>
+__global__ void __launch_bounds__(SMALL_THREADS)
+k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__restrict__ loc,
+               const u32 *__restrict__ rank, const double *__restrict__ uniq, ll N, int ndim,
+               const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
+               const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
+               int *__restrict__ part) {
+  extern __shared__ __align__(16) unsigned char pss_smem[];
+  unsigned short *buf = reinterpret_cast<unsigned short *>(pss_smem);  // 4 list buffers
+  unsigned short *cl = buf + 4 * SMALL_MAX;                             // prefix counts
+  unsigned short *spl = cl + SMALL_MAX;  // lower child's size by sub-range start
+  unsigned char *side = reinterpret_cast<unsigned char *>(spl + SMALL_MAX);
+  unsigned char *sax = side + SMALL_MAX;  // cut axis by sub-range start
+  __shared__ int wsum[SMALL_WARPS];
+  __shared__ int lb[4];  // buffer of each list (lb[3]: the spare)
+  const ll sg = blockIdx.x;
+  const ll start = seg_start[sg];
+  const int n = (int)seg_n[sg], p0 = seg_p[sg], r0 = seg_r0[sg];
+  if (n <= 0 || p0 <= 0) return;
+  const bool seg_act = p0 > 1 || (LOCAL && p0 == 1 && n >= 2);
+  if (!seg_act || n > SMALL_MAX) {
+    if (part && n <= SMALL_MAX && p0 == 1)
+      for (int x = threadIdx.x; x < n; x += blockDim.x) part[perm[start + x]] = r0;
+    return;
+  }
+  const int *gl0 = lists + start;  // local id k -> element gl0[k]
+  for (int x = threadIdx.x; x < n; x += blockDim.x) loc[gl0[x]] = x;
+  __syncthreads();
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    buf[x] = (unsigned short)x;
+    for (int d = 1; d < ndim; d++)
+      buf[d * SMALL_MAX + x] = (unsigned short)loc[lists[(ll)d * N + start + x]];
+  }
+  if (threadIdx.x < 4) lb[threadIdx.x] = threadIdx.x < ndim ? threadIdx.x : 3;
+  __syncthreads();
+  if (p0 == 1)
+    pss_levels<LOCAL, true>(perm, gl0, rank, uniq, N, ndim, start, n, p0, r0, part, buf, cl, spl,
+                            side, sax, wsum, lb);
+  else
+    pss_levels<LOCAL, false>(perm, gl0, rank, uniq, N, ndim, start, n, p0, r0, part, buf, cl,
+                             spl, side, sax, wsum, lb);
 }
 
 static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_local,
