@@ -18,13 +18,16 @@
 // 28-31).  The Laplacian is applied in difference form y_i = sum_j w_ij
 // (x_i - x_j) (exact integer weights).  Lanczos vectors are FP64 or FP32;
 // every dot product, the tridiagonal matrix and the eigensolve are FP64.
-// Dot products reduce per 2048-row tile (fixed tree) and then per group
-// over its tiles (fixed order), so results are bitwise repeatable.
+// Dot products reduce per tile (512 to 8192 rows by the group's size; fixed
+// trees) and then per group over its tiles (fixed order), so results are
+// bitwise repeatable.  With FP32 vectors the residual check forms L f
+// exactly in 64-bit fixed point.
 #include <math.h>
 
 #include <algorithm>
-#include <chrono>
 #include <array>
+#include <atomic>
+#include <chrono>
 
 #include "rsb.cuh"
 #include "warm.cuh"
@@ -2536,8 +2539,9 @@ struct Lanczos {
       const char *e = getenv("PARRSB_GPU_DEVICE_LOOP");
       return !(e && atoi(e) == 0);
     }();
-    static bool device_loop_broken = false;
-    static bool persist_broken = false;  // a graph with k_steps failed here once
+    // sticky fallbacks after a graph could not be built (any thread, any device)
+    static std::atomic<bool> device_loop_broken{false};
+    static std::atomic<bool> persist_broken{false};  // a graph with k_steps failed once
     persist = !persist_broken && want_persist();
     for (int attempt = 0;
          attempt < 2 && !exec && use_graph && ev.empty() && device_loop_env && !device_loop_broken;
