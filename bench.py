@@ -290,8 +290,10 @@ def _time_device(fn, reps=3):
 def other_rows(P, meshgen, lib, torch, ctypes, np):
     """RCB / RIB of the 512x512 quad annulus (262,144 elements) to 1024 parts,
     gencon on the same annulus (the reference algorithm's element check
-    fails there) and on a 128x128x64 jittered hex box (8.4M corner points);
-    device-resident inputs, best of 3 after a warm-up."""
+    fails there) and on a 128x128x64 jittered hex box (8.4M corner points),
+    the batched level solve of 4,096 subgraphs, and RSB of the 128x128x64
+    annular pipe into 256 parts in both precisions; device-resident inputs,
+    best of 3 after a warm-up."""
     from parrsb_gb300.options import ParrsbOptions
     out = {}
     vtx, xyz = meshgen.annulus_quad(512, 512, amp=0.02, seed=0)
@@ -337,6 +339,38 @@ def other_rows(P, meshgen, lib, torch, ctypes, np):
     c4["components_max"] = int(P.components(vc, sc, 4096).max())
     out["c4_batched_level_solve"] = c4
     del vc, sc
+    # RSB of the 128x128x64 annular pipe (1,048,576 elements) into 256 parts,
+    # FP32 and FP64 Lanczos vectors, the benchmark's method; the oracle's cut
+    # of the same input from the committed fixture
+    vp, xp = meshgen.pipe_hex(128, 128, 64, jitter=0.05, seed=0)
+    dvp, dxp = torch.from_numpy(vp).cuda(), torch.from_numpy(xp).cuda()
+    dpp = torch.empty(len(vp), dtype=torch.int32, device="cuda")
+    with open(os.path.join(ROOT, "tests", "golden", "rsb_hex_pipe_128x128x64_to_256.json")) as fh:
+        fx = json.load(fh)
+    c3 = {"elements": int(len(vp)), "nparts": 256, "oracle_weighted_cut": fx["weighted_cut"]}
+    saved = os.environ.get("PARRSB_GPU_FP32")
+    for name, fp32 in (("fp32", "1"), ("fp64", "0")):
+        os.environ["PARRSB_GPU_FP32"] = fp32
+
+        def runp():
+            o = ParrsbOptions.make(partitioner=0, verbose_level=0)
+            rc = lib.parrsb_part_mesh_device(ctypes.c_void_p(dpp.data_ptr()),
+                                             ctypes.c_void_p(dvp.data_ptr()),
+                                             ctypes.c_void_p(dxp.data_ptr()), len(vp), 8,
+                                             ctypes.byref(o), 256)
+            assert rc == 0
+        t = _time_device(runp)
+        stp = P.last_stats()
+        cut = P.part_quality(dpp.cpu().numpy(), vp, 256)[0]
+        c3[name] = {"s": t, "weighted_cut": cut, "cut_over_oracle": cut / fx["weighted_cut"],
+                    "max_fiedler_resid": stp.max_fiedler_resid,
+                    "lanczos_steps": int(stp.lanczos_iters)}
+    if saved is None:
+        os.environ.pop("PARRSB_GPU_FP32", None)
+    else:
+        os.environ["PARRSB_GPU_FP32"] = saved
+    out["c3_pipe_128x128x64_to_256"] = c3
+    del vp, xp, dvp, dxp, dpp
     _, xyz3 = meshgen.box_hex(128, 128, 64, jitter=0.1, seed=0)
     d3 = torch.from_numpy(xyz3).cuda()
     ids3 = torch.empty(xyz3.shape[0] * 8, dtype=torch.int64, device="cuda")
