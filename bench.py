@@ -637,6 +637,11 @@ def main():
     peak, peak_kind = load_peaks()
     traffic = load_traffic()
     per_launch_bytes = spmv_bytes / spmv_launches if spmv_launches else None
+    # the whole pass graph: SpMV bytes plus the vector updates' 3 x 4 B per
+    # row and step each (FP32), over the pass graphs' device time
+    vec_bytes = 2 * 3 * 4 * sum(x.lanczos_row_iters for x in stats)
+    pass_ms = sum(x.lanczos_ms[5] for x in stats)
+    pass_gbs = (spmv_bytes + vec_bytes) / (pass_ms / 1e3) / 1e9 if pass_ms > 0 else None
     tr_val = None
     if traffic and per_launch_bytes:
         tr_val = traffic.get("dram_bytes_per_algorithmic_byte", None)
@@ -697,7 +702,13 @@ def main():
                      "spmv_ms_per_launch": spmv_ms / spmv_launches if spmv_launches else None,
                      "timed_on": "one step after the timed region, CUDA events around every "
                                  "SpMV launch inside the Lanczos graphs",
-                     "algorithmic_bytes_per_launch": per_launch_bytes},
+                     "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "pass_graphs": {"achieved": pass_gbs,
+                                     "frac": (pass_gbs / peak) if pass_gbs else None,
+                                     "what": ("SpMV plus P / R update bytes of every Lanczos "
+                                              "step over the pass graphs' device time "
+                                              "(eigensolves, Ritz vectors, finalisations "
+                                              "and residual checks included)")}},
         "cpu_baseline": cpu,
         "plain_gpu": plain,
         "start_vectors": starts,
