@@ -224,7 +224,20 @@ __global__ void k_mp_scales(const double *__restrict__ part, const int *__restri
 // per tile: sum of (c - o), sum of (c - o)(c - o)^T (6) about the group's
 // origin o = centroid of its first position (numerically safe raw moments),
 // coordinates in element spacings; and the tile's bounding box of the raw
-// centroids (min x y z, max x y z), from which RCB picks its cut axis
+// centroids (min x y z, max x y z), from which RCB picks its cut axis.
+// Each thread accumulates its elements' terms in FP32 (c - o in FP64 first,
+// so any coordinate range is safe; 64 elements per thread), the block sums
+// its threads in FP64: FP64 arithmetic per element, at 1/64 of the FP32
+// rate, bounded this kernel.  The box is kept on order-preserving integer
+// keys of the doubles (the integer pipe).
+__device__ __forceinline__ unsigned long long mp_okey(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double mp_okey_inv(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k));
+}
+
 __global__ void __launch_bounds__(256)
 k_mp_moments(const FTile *__restrict__ tiles, const ll *__restrict__ gstart,
              const int *__restrict__ perm, const double *__restrict__ cent, ll nel,
@@ -234,39 +247,45 @@ k_mp_moments(const FTile *__restrict__ tiles, const ll *__restrict__ gstart,
   const int e0 = perm[gstart[t.g]];
   const double o[3] = {cent[e0], cent[nel + e0], cent[2 * nel + e0]};
   const double *k = sa + (ll)t.g * 3;
-  double s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  double lo[3] = {o[0], o[1], o[2]}, hi[3] = {o[0], o[1], o[2]};
+  const float kf[3] = {(float)k[0], (float)k[1], (float)k[2]};
+  float s[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long lo[3], hi[3];
+  for (int a = 0; a < 3; a++) lo[a] = hi[a] = mp_okey(o[a]);
   for (ll i = t.b + threadIdx.x; i < t.e; i += blockDim.x) {
     const int e = perm[i];
     const double c[3] = {cent[e], cent[nel + e], cent[2 * nel + e]};
-    const double x = (c[0] - o[0]) * k[0], y = (c[1] - o[1]) * k[1], z = (c[2] - o[2]) * k[2];
+    const float x = (float)(c[0] - o[0]) * kf[0], y = (float)(c[1] - o[1]) * kf[1],
+                z = (float)(c[2] - o[2]) * kf[2];
     s[0] += x, s[1] += y, s[2] += z;
-    s[3] += x * x, s[4] += y * y, s[5] += z * z;
-    s[6] += x * y, s[7] += x * z, s[8] += y * z;
-    for (int a = 0; a < 3; a++) lo[a] = fmin(lo[a], c[a]), hi[a] = fmax(hi[a], c[a]);
+    s[3] = fmaf(x, x, s[3]), s[4] = fmaf(y, y, s[4]), s[5] = fmaf(z, z, s[5]);
+    s[6] = fmaf(x, y, s[6]), s[7] = fmaf(x, z, s[7]), s[8] = fmaf(y, z, s[8]);
+    for (int a = 0; a < 3; a++) {
+      const unsigned long long q = mp_okey(c[a]);
+      lo[a] = min(lo[a], q), hi[a] = max(hi[a], q);
+    }
   }
   __shared__ double sh[32];
   for (int q = 0; q < 9; q++) {
-    const double v = mp_block_sum(s[q], sh);
+    const double v = mp_block_sum((double)s[q], sh);
     if (threadIdx.x == 0) part[(ll)blockIdx.x * 9 + q] = v;
     __syncthreads();
   }
   // the box: o lies in the group, so starting from it leaves min / max exact
-  __shared__ double bx[6][8];
+  __shared__ unsigned long long bx[6][8];
   for (int a = 0; a < 3; a++) {
     for (int off = 16; off > 0; off >>= 1) {
-      lo[a] = fmin(lo[a], __shfl_down_sync(0xffffffffu, lo[a], off));
-      hi[a] = fmax(hi[a], __shfl_down_sync(0xffffffffu, hi[a], off));
+      lo[a] = min(lo[a], __shfl_down_sync(0xffffffffu, lo[a], off));
+      hi[a] = max(hi[a], __shfl_down_sync(0xffffffffu, hi[a], off));
     }
   }
   if ((threadIdx.x & 31) == 0)
     for (int a = 0; a < 3; a++) bx[a][threadIdx.x >> 5] = lo[a], bx[3 + a][threadIdx.x >> 5] = hi[a];
   __syncthreads();
   if (threadIdx.x < 6) {
-    double v = bx[threadIdx.x][0];
+    unsigned long long v = bx[threadIdx.x][0];
     for (int w = 1; w < (int)(blockDim.x >> 5); w++)
-      v = threadIdx.x < 3 ? fmin(v, bx[threadIdx.x][w]) : fmax(v, bx[threadIdx.x][w]);
-    box[(ll)blockIdx.x * 6 + threadIdx.x] = v;
+      v = threadIdx.x < 3 ? min(v, bx[threadIdx.x][w]) : max(v, bx[threadIdx.x][w]);
+    box[(ll)blockIdx.x * 6 + threadIdx.x] = mp_okey_inv(v);
   }
 }
 
@@ -965,7 +984,9 @@ __global__ void k_mp_feat_to_elem(const int *__restrict__ perm, const float *__r
 }
 
 // Geometric start: y = -sin(pi x~_1 / 2) along the group's principal axis,
-// the Fiedler vector of a uniform bar (a cosine over its length); FP64.
+// the Fiedler vector of a uniform bar (a cosine over its length).  x~_1 in
+// FP64 (its axis only), the sine in FP32 (sinpif): a start vector needs no
+// more, and FP64 transcendentals at 1/64 of the FP32 rate bounded this pass.
 __global__ void k_mp_geometric(const int *__restrict__ perm, const int *__restrict__ grp,
                                const double *__restrict__ cent, ll nel,
                                const double *__restrict__ frame, ll N, double *__restrict__ y) {
@@ -975,9 +996,11 @@ __global__ void k_mp_geometric(const int *__restrict__ perm, const int *__restri
   double v = 0.0;
   if (g >= 0) {
     const int e = perm[i];
-    double xt[3];
-    frame_coords(frame + (ll)g * MP_FRAME, cent, nel, e, xt);
-    v = -sin(1.5707963267948966 * xt[0]);
+    const double *f = frame + (ll)g * MP_FRAME;
+    const double x = fma(cent[e], f[13], -f[0]), yy = fma(cent[nel + e], f[14], -f[1]),
+                 z = fma(cent[2 * nel + e], f[15], -f[2]);
+    const double x1 = fma(f[3], x, fma(f[4], yy, f[5] * z)) * f[12];
+    v = -(double)sinpif(0.5f * (float)x1);
   }
   y[i] = v;
 }

@@ -54,8 +54,11 @@ def test_features_match_restatement():
     b.close()
     rows, col, w = _graph(vtx, group)
     Xo = W.features(O.centroids(xyz, 8), group.astype(np.int64), rows, col, w)
-    # FP32 features computed in FP64 (Jacobi frames on the GPU, LAPACK here)
-    np.testing.assert_allclose(X[:, :5], Xo[:, :5], rtol=1e-5, atol=1e-6)
+    # FP32 features; the GPU's group frames come from moments accumulated in
+    # FP32 per thread (FP64 across threads; Jacobi on the GPU, LAPACK here),
+    # so positions agree to a few 1e-5, below the 16 significant bits the
+    # first layer keeps of them (a high and a low BF16 part)
+    np.testing.assert_allclose(X[:, :5], Xo[:, :5], rtol=1e-5, atol=3e-5)
     assert np.all(X[:, 5:] == 0)
 
 
