@@ -92,10 +92,10 @@ __global__ void k_scatter_inv(const int *__restrict__ vals, ll n, int *__restric
 // FILL = true: columns and weights at rowptr[a].
 constexpr int GR_WARPS = 4;
 constexpr int GR_CAP = 256;
-constexpr int GR_HASH = 512;  // power of two, twice GR_CAP: probe chains stay short
+constexpr int GR_HASH = 256;  // power of two >= GR_CAP: more slots than distinct keys
 
 __device__ __forceinline__ int gr_slot0(int b) {
-  return (int)(((unsigned)b * 2654435761u) >> 23);  // Fibonacci hashing to 9 bits
+  return (int)(((unsigned)b * 2654435761u) >> 24);  // Fibonacci hashing to 8 bits
 }
 
 template <bool FILL>
@@ -115,22 +115,23 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
   int wmax = 0;
   if (a < N) {  // warp-uniform
     // run of each vertex of a (lane k < nv), then every lane holds all of them
-    ll rs = 0, rl = 0;
+    // (slot positions and candidate counts fit 32 bits: N < 2^28, nv <= 8)
+    int rs = 0, rl = 0;
     if (lane < nv) {
       const int r = runid[inv[a * nv + lane]];
-      rs = run_start[r];
-      rl = run_start[r + 1] - rs;
+      rs = (int)run_start[r];
+      rl = (int)(run_start[r + 1] - run_start[r]);
     }
-    ll RS[8], EX[8];
-    ll C = 0;
+    int RS[8], EX[8];
+    int C = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       RS[k] = __shfl_sync(0xffffffffu, rs, k);
       EX[k] = C;
       C += __shfl_sync(0xffffffffu, rl, k);  // lanes >= nv hold 0
     }
-    auto cand_at = [&](ll t) -> int {  // element of candidate t
-      ll base = RS[0] - EX[0];
+    auto cand_at = [&](int t) -> int {  // element of candidate t
+      int base = RS[0] - EX[0];
 #pragma unroll
       for (int k = 1; k < 8; k++)
         if (k < nv && t >= EX[k]) base = RS[k] - EX[k];
@@ -138,12 +139,12 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
     };
     const bool staged = C <= GR_CAP;
     if (staged) {
-      for (ll t = lane; t < C; t += 32) {
+      for (int t = lane; t < C; t += 32) {
         const int b = cand_at(t);
         cand[wid][t] = b;
         if (b == (int)a) continue;
         int h = gr_slot0(b);
-        for (;;) {  // at most C distinct keys in GR_HASH > C slots: a free or equal slot exists
+        for (;;) {  // fewer distinct keys than slots (a != b): a free or equal slot exists
           const int prev = atomicCAS(&hkey[wid][h], -1, b);
           if (prev == -1 || prev == b) break;
           h = (h + 1) & (GR_HASH - 1);
@@ -154,8 +155,8 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
       __syncwarp();
     }
     ll out = 0;
-    for (ll t0 = 0; t0 < C; t0 += 32) {
-      const ll t = t0 + lane;
+    for (int t0 = 0; t0 < C; t0 += 32) {
+      const int t = t0 + lane;
       bool first = false;
       int b = -1, cnt = 0;
       if (t < C) {
@@ -168,7 +169,7 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
             first = hfirst[wid][h] == (int)t;
           } else {
             int before = 0;  // occurrences of b ahead of t
-            for (ll j = 0; j < C; j++) {
+            for (int j = 0; j < C; j++) {
               const int m = cand_at(j) == b;
               cnt += m;
               before += m & (j < t);
@@ -194,7 +195,7 @@ k_graph_rows(int nv, ll N, const int *__restrict__ sorted_slot, const int *__res
       int hs[GR_CAP / 32];
 #pragma unroll
       for (int k = 0; k < GR_CAP / 32; k++) {
-        const ll t = lane + 32 * k;
+        const int t = lane + 32 * k;
         hs[k] = -1;
         if (t < C) {
           const int b = cand[wid][t];
@@ -237,6 +238,9 @@ __global__ void k_inv_perm(const int *__restrict__ perm, ll N, int *__restrict__
   if (i < N) inv[perm[i]] = (int)i;
 }
 
+// The level-matrix kernels walk a dual-graph row per thread through two
+// dependent gathers per entry (position inv[col], its group); eight entries
+// at a time keep eight of each in flight instead of one.
 __global__ void k_ell_count(const int *__restrict__ perm, const int *__restrict__ inv,
                             const int *__restrict__ grp, const ll *__restrict__ rowptr,
                             const int *__restrict__ col, ll N, int *__restrict__ rowlen) {
@@ -246,8 +250,16 @@ __global__ void k_ell_count(const int *__restrict__ perm, const int *__restrict_
   int cnt = 0;
   if (g >= 0) {
     int a = perm[i];
-    for (ll q = rowptr[a]; q < rowptr[a + 1]; q++)
-      if (grp[inv[col[q]]] == g) cnt++;
+    const ll q0 = rowptr[a], q1 = rowptr[a + 1];
+    ll q = q0;
+    for (; q + 8 <= q1; q += 8) {
+      int j[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) j[u] = inv[col[q + u]];
+#pragma unroll
+      for (int u = 0; u < 8; u++) cnt += grp[j[u]] == g;
+    }
+    for (; q < q1; q++) cnt += grp[inv[col[q]]] == g;
   }
   rowlen[i] = cnt;
 }
@@ -286,7 +298,22 @@ __global__ void k_ell_fill(const int *__restrict__ perm, const int *__restrict__
   int g = grp[i];
   if (g >= 0) {
     int a = perm[i];
-    for (ll q = rowptr[a]; q < rowptr[a + 1]; q++) {
+    const ll q0 = rowptr[a], q1 = rowptr[a + 1];
+    ll q = q0;
+    for (; q + 8 <= q1; q += 8) {  // same entries in the same order, eight gathers in flight
+      int j[8], gj[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) j[u] = inv[col[q + u]];
+#pragma unroll
+      for (int u = 0; u < 8; u++) gj[u] = grp[j[u]];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+        if (gj[u] == g) {
+          out[(ll)k * 32] = (unsigned)j[u] | ((unsigned)w[q + u] << 28);
+          k++;
+        }
+    }
+    for (; q < q1; q++) {
       int j = inv[col[q]];
       if (grp[j] == g) {
         out[(ll)k * 32] = (unsigned)j | ((unsigned)w[q] << 28);
