@@ -1200,50 +1200,54 @@ __global__ void k_ps_final(const int *__restrict__ lists, ll N, const int *__res
 // every active sub-range (tracked per position in registers as k_rcb_small
 // does): its cut axis from the first and last entry of each list, the side
 // of each element from the cut axis' list, and a stable partition of every
-// list by side (a CTA-wide prefix count).  Same tree, same order as the
-// sort-per-level kernels; without LOCAL a sub-range that is no longer cut
-// keeps the list of the axis that cut it last.
-constexpr size_t pss_smem_bytes() {  // 4 lists, prefix counts, splits (u16); side, axis (u8)
-  return (size_t)SMALL_MAX * (6 * sizeof(unsigned short) + 2);
+// list by side.  The partition counts lower flags with one warp ballot per
+// 32 positions: the count before a position is the totals of the warps
+// before its warp (a shuffle scan), the totals of the rounds before its
+// round inside its warp, and the ballot's bits below its lane.  All three
+// lists move to three spare buffers in the same pass, so a level takes four
+// CTA barriers.  Same tree, same order as the sort-per-level kernels;
+// without LOCAL a sub-range that is no longer cut keeps the list of the axis
+// that cut it last.
+constexpr int SMALL_ROUNDS = SMALL_MAX / 32;  // ballots per list
+constexpr size_t pss_smem_bytes() {
+  // local id -> element (int); six list buffers and the lower child's size
+  // by sub-range start (u16); side and cut axis (u8); per list the ballots
+  // (u32) and the in-warp prefix of each round (u16)
+  return (size_t)SMALL_MAX * (sizeof(int) + 7 * sizeof(unsigned short) + 2) +
+         (size_t)3 * SMALL_ROUNDS * (sizeof(u32) + sizeof(unsigned short));
 }
 
-__device__ __forceinline__ int pss_excl_scan(int v, int *wsum) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) wsum[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    int s = wsum[lane];  // SMALL_WARPS == 32
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, s, o);
-      if (lane >= o) s += y;
-    }
-    wsum[lane] = s;
-  }
-  __syncthreads();
-  const int r = (warp ? wsum[warp - 1] : 0) + x - v;
-  __syncthreads();
-  return r;
+struct PssSmem {
+  int *gl;               // local id -> element
+  u32 *bal;              // [3][SMALL_ROUNDS] lower flags, one word per 32 positions
+  unsigned short *buf;   // [6][SMALL_MAX]: three lists and three spares
+  unsigned short *spl;   // lower child's size by sub-range start
+  unsigned short *wpre;  // [3][SMALL_ROUNDS] lower flags before the round in its warp
+  unsigned char *side;   // side by local id
+  unsigned char *sax;    // cut axis by sub-range start
+};
+
+__device__ __forceinline__ PssSmem pss_carve(unsigned char *s) {
+  PssSmem m;
+  m.gl = reinterpret_cast<int *>(s);
+  m.bal = reinterpret_cast<u32 *>(m.gl + SMALL_MAX);
+  m.buf = reinterpret_cast<unsigned short *>(m.bal + 3 * SMALL_ROUNDS);
+  m.spl = m.buf + 6 * SMALL_MAX;
+  m.wpre = m.spl + SMALL_MAX;
+  m.side = reinterpret_cast<unsigned char *>(m.wpre + 3 * SMALL_ROUNDS);
+  m.sax = m.side + SMALL_MAX;
+  return m;
 }
 
 // The level loop of k_rcb_small_ps; PONE: the segment has one virtual rank
 // (only the local halving: no rank counts to track, every part is r0).
 template <bool LOCAL, bool PONE>
-__device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__restrict__ gl0,
-                                           const u32 *__restrict__ rank,
-                                           const double *__restrict__ uniq, ll N, int ndim,
-                                           ll start, int n, int p0, int r0,
-                                           int *__restrict__ part, unsigned short *buf,
-                                           unsigned short *cl, unsigned short *spl,
-                                           unsigned char *side, unsigned char *sax, int *wsum,
-                                           int *lb) {
+__device__ __forceinline__ void pss_levels(int *__restrict__ perm, const double *__restrict__ cent,
+                                           ll N, int ndim, ll start, int n, int p0, int r0,
+                                           int *__restrict__ part, const PssSmem &m,
+                                           int (*wsum)[SMALL_WARPS]) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const u32 lt = (1u << lane) - 1u;
   // sub-range of each own position (start | length << 16), its virtual
   // ranks, and the axis that cut it last
   u32 sl_r[SMALL_ITEMS];
@@ -1254,6 +1258,7 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
     sl_r[r] = (u32)n << 16, oax_r[r] = -1;
     if (!PONE) p_r[r] = p0, rk_r[r] = 0;
   }
+  int cur = 0;  // the lists are in buffers 3 cur .. 3 cur + 2, the spares in the others
   for (int d = 0; d < 64; d++) {
     if (d > 0) {  // advance every position's sub-range by the previous cut
 #pragma unroll
@@ -1261,8 +1266,8 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
         const int x = warp * SMALL_SPAN + r * 32 + lane;
         int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16), p = PONE ? 1 : p_r[r];
         if (!(p > 1 || (LOCAL && ln >= 2))) continue;  // no longer cut
-        const int L = spl[st], h = p > 1 ? (p + 1) / 2 : 0;
-        oax_r[r] = (signed char)sax[st];
+        const int L = m.spl[st], h = p > 1 ? (p + 1) / 2 : 0;
+        oax_r[r] = (signed char)m.sax[st];
         if (x < st + L) {
           ln = L;
           p = p > 1 ? h : p;
@@ -1276,7 +1281,6 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
         if (!PONE) p_r[r] = p;
       }
     }
-    __syncthreads();  // every sax read above is done
     u32 act = 0;
 #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
@@ -1284,26 +1288,32 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
       const int ln = (int)(sl_r[r] >> 16);
       if (x < n && ((!PONE && p_r[r] > 1) || (LOCAL && ln >= 2))) act |= 1u << r;
     }
+    // barrier: the reads of sax and spl above and the previous level's
+    // partition are done before the cut axes are written and the lists read
     if (!__syncthreads_or(act != 0)) break;
-    // cut axis of each active sub-range: the ranks of the first and last
-    // entry of each list
+    const unsigned short *Lc = m.buf + 3 * cur * SMALL_MAX;   // current lists
+    unsigned short *Ls = m.buf + 3 * (cur ^ 1) * SMALL_MAX;  // spares
+    // cut axis of each active sub-range: the coordinates of the first and
+    // last entry of each list
 #pragma unroll
     for (int r = 0; r < SMALL_ITEMS; r++) {
       const int x = warp * SMALL_SPAN + r * 32 + lane;
       const int st = (int)(sl_r[r] & 0xFFFFu), ln = (int)(sl_r[r] >> 16);
       if (!((act >> r) & 1u) || x != st) continue;
       double len[3] = {0.0, 0.0, 0.0};
-      for (int q = 0; q < ndim; q++) {
-        const unsigned short *Lq = buf + lb[q] * SMALL_MAX;
-        const u32 lo = rank[(ll)q * N + gl0[Lq[st]]], hi = rank[(ll)q * N + gl0[Lq[st + ln - 1]]];
-        len[q] = __dsub_rn(uniq[(ll)q * N + hi], uniq[(ll)q * N + lo]);
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        if (q >= ndim) break;
+        const unsigned short *Lq = Lc + q * SMALL_MAX;
+        const int lo = m.gl[Lq[st]], hi = m.gl[Lq[st + ln - 1]];
+        len[q] = __dsub_rn(cent[(ll)q * N + hi], cent[(ll)q * N + lo]);
       }
       int ax = 0;
       for (int q = 1; q < ndim; q++)
         if (len[q] > len[ax]) ax = q;
-      sax[st] = (unsigned char)ax;
+      m.sax[st] = (unsigned char)ax;
       const int p = PONE ? 1 : p_r[r];
-      spl[st] = (unsigned short)(p > 1 ? lower_count_small(ln, p) : ln / 2);
+      m.spl[st] = (unsigned short)(p > 1 ? lower_count_small(ln, p) : ln / 2);
     }
     __syncthreads();
     // side of every element of a cut sub-range, from the cut axis' list
@@ -1312,79 +1322,76 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
       if (!((act >> r) & 1u)) continue;
       const int x = warp * SMALL_SPAN + r * 32 + lane;
       const int st = (int)(sl_r[r] & 0xFFFFu);
-      side[buf[lb[sax[st]] * SMALL_MAX + x]] = (x - st) >= (int)spl[st] ? 1 : 0;
+      m.side[Lc[m.sax[st] * SMALL_MAX + x]] = (x - st) >= (int)m.spl[st] ? 1 : 0;
     }
     __syncthreads();
-    // stable partition of each list by side, into the spare buffer
+    // lower flags of every list: one ballot per round of 32 positions, the
+    // in-warp prefix of each round and each warp's total
     for (int q = 0; q < ndim; q++) {
-      const unsigned short *Lq = buf + lb[q] * SMALL_MAX;
-      unsigned short *Tq = buf + lb[3] * SMALL_MAX;
-      // lower flag by position (written by the thread that tracks the
-      // position's sub-range, read back in contiguous runs for the scan)
+      const unsigned short *Lq = Lc + q * SMALL_MAX;
+      int cnt = 0;
 #pragma unroll
       for (int r = 0; r < SMALL_ITEMS; r++) {
         const int x = warp * SMALL_SPAN + r * 32 + lane;
-        if (x >= n) continue;
+        const bool f = ((act >> r) & 1u) && m.side[Lq[x]] == 0;  // act implies x < n
+        const u32 b = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) {
+          m.bal[q * SMALL_ROUNDS + warp * SMALL_ITEMS + r] = b;
+          m.wpre[q * SMALL_ROUNDS + warp * SMALL_ITEMS + r] = (unsigned short)cnt;
+        }
+        cnt += __popc(b);
+      }
+      if (lane == 0) wsum[q][warp] = cnt;
+    }
+    __syncthreads();
+    // stable partition of each list by side into its spare buffer; a
+    // position outside a cut sub-range keeps its place
+    for (int q = 0; q < ndim; q++) {
+      const int wv = wsum[q][lane];  // SMALL_WARPS == 32
+      int inc = wv;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+      }
+      const int exc = inc - wv;  // lane w: lower flags of the warps before w
+      const int base_x = __shfl_sync(0xffffffffu, exc, warp);
+      const unsigned short *Lq = Lc + q * SMALL_MAX;
+      unsigned short *Tq = Ls + q * SMALL_MAX;
+      const u32 *bq = m.bal + q * SMALL_ROUNDS;
+      const unsigned short *wq = m.wpre + q * SMALL_ROUNDS;
+#pragma unroll
+      for (int r = 0; r < SMALL_ITEMS; r++) {
+        const int x = warp * SMALL_SPAN + r * 32 + lane;
         const bool a = (act >> r) & 1u;
-        cl[x] = (unsigned short)(a ? (side[Lq[x]] == 0 ? 1 : 0) : 1);
-      }
-      __syncthreads();
-      int v[SMALL_ITEMS], c = 0;
-#pragma unroll
-      for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = threadIdx.x * SMALL_ITEMS + r;
-        v[r] = x < n ? (int)cl[x] : 0;
-        c += v[r];
-      }
-      int run = pss_excl_scan(c, wsum);
-#pragma unroll
-      for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = threadIdx.x * SMALL_ITEMS + r;
-        if (x < n) cl[x] = (unsigned short)run;  // lower flags before x (x < 8192)
-        run += v[r];
-      }
-      __syncthreads();
-#pragma unroll
-      for (int r = 0; r < SMALL_ITEMS; r++) {
-        const int x = warp * SMALL_SPAN + r * 32 + lane;
+        const int st = a ? (int)(sl_r[r] & 0xFFFFu) : x;
+        const int base_st = __shfl_sync(0xffffffffu, exc, st / SMALL_SPAN);
         if (x >= n) continue;
-        int dest = x;
         const unsigned short id = Lq[x];
-        if ((act >> r) & 1u) {
-          const int st = (int)(sl_r[r] & 0xFFFFu), L = spl[st];
-          const int before = (int)cl[x] - (int)cl[st];
-          dest = side[id] == 0 ? st + before : st + L + (x - st - before);
+        int dest = x;
+        if (a) {
+          const int k = warp * SMALL_ITEMS + r, ks = st >> 5;
+          const u32 bx = bq[k];
+          const int before = (base_x + (int)wq[k] + __popc(bx & lt)) -
+                             (base_st + (int)wq[ks] + __popc(bq[ks] & ((1u << (st & 31)) - 1u)));
+          dest = ((bx >> lane) & 1u) ? st + before : st + (int)m.spl[st] + (x - st - before);
         }
         Tq[dest] = id;
       }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        const int t2 = lb[3];
-        lb[3] = lb[q];
-        lb[q] = t2;
-      }
-      __syncthreads();
     }
+    cur ^= 1;
   }
   // order: a LOCAL recursion ends in single elements (every list agrees);
   // otherwise each position takes the list of the axis that cut it last
-  int ev[SMALL_ITEMS];
+  const unsigned short *Lc = m.buf + 3 * cur * SMALL_MAX;
 #pragma unroll
   for (int r = 0; r < SMALL_ITEMS; r++) {
     const int x = warp * SMALL_SPAN + r * 32 + lane;
-    ev[r] = 0;
     if (x < n) {
       const int a = oax_r[r] < 0 ? 0 : oax_r[r];
-      ev[r] = gl0[buf[lb[a] * SMALL_MAX + x]];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < SMALL_ITEMS; r++) {
-    const int x = warp * SMALL_SPAN + r * 32 + lane;
-    if (x < n) {
-      perm[start + x] = ev[r];
-      if (part) part[ev[r]] = r0 + (PONE ? 0 : rk_r[r]);
+      const int e = m.gl[Lc[a * SMALL_MAX + x]];
+      perm[start + x] = e;
+      if (part) part[e] = r0 + (PONE ? 0 : rk_r[r]);
     }
   }
 }
@@ -1392,18 +1399,13 @@ __device__ __forceinline__ void pss_levels(int *__restrict__ perm, const int *__
 template <bool LOCAL>
 __global__ void __launch_bounds__(SMALL_THREADS)
 k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__restrict__ loc,
-               const u32 *__restrict__ rank, const double *__restrict__ uniq, ll N, int ndim,
+               const double *__restrict__ cent, ll N, int ndim,
                const ll *__restrict__ seg_start, const ll *__restrict__ seg_n,
                const int *__restrict__ seg_p, const int *__restrict__ seg_r0,
                int *__restrict__ part) {
   extern __shared__ __align__(16) unsigned char pss_smem[];
-  unsigned short *buf = reinterpret_cast<unsigned short *>(pss_smem);  // 4 list buffers
-  unsigned short *cl = buf + 4 * SMALL_MAX;                             // prefix counts
-  unsigned short *spl = cl + SMALL_MAX;  // lower child's size by sub-range start
-  unsigned char *side = reinterpret_cast<unsigned char *>(spl + SMALL_MAX);
-  unsigned char *sax = side + SMALL_MAX;  // cut axis by sub-range start
-  __shared__ int wsum[SMALL_WARPS];
-  __shared__ int lb[4];  // buffer of each list (lb[3]: the spare)
+  const PssSmem m = pss_carve(pss_smem);
+  __shared__ int wsum[3][SMALL_WARPS];
   const ll sg = blockIdx.x;
   const ll start = seg_start[sg];
   const int n = (int)seg_n[sg], p0 = seg_p[sg], r0 = seg_r0[sg];
@@ -1415,25 +1417,26 @@ k_rcb_small_ps(int *__restrict__ perm, const int *__restrict__ lists, int *__res
     return;
   }
   const int *gl0 = lists + start;  // local id k -> element gl0[k]
-  for (int x = threadIdx.x; x < n; x += blockDim.x) loc[gl0[x]] = x;
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    const int e = gl0[x];
+    loc[e] = x;
+    m.gl[x] = e;
+  }
   __syncthreads();
   for (int x = threadIdx.x; x < n; x += blockDim.x) {
-    buf[x] = (unsigned short)x;
+    m.buf[x] = (unsigned short)x;
     for (int d = 1; d < ndim; d++)
-      buf[d * SMALL_MAX + x] = (unsigned short)loc[lists[(ll)d * N + start + x]];
+      m.buf[d * SMALL_MAX + x] = (unsigned short)loc[lists[(ll)d * N + start + x]];
   }
-  if (threadIdx.x < 4) lb[threadIdx.x] = threadIdx.x < ndim ? threadIdx.x : 3;
   __syncthreads();
   if (p0 == 1)
-    pss_levels<LOCAL, true>(perm, gl0, rank, uniq, N, ndim, start, n, p0, r0, part, buf, cl, spl,
-                            side, sax, wsum, lb);
+    pss_levels<LOCAL, true>(perm, cent, N, ndim, start, n, p0, r0, part, m, wsum);
   else
-    pss_levels<LOCAL, false>(perm, gl0, rank, uniq, N, ndim, start, n, p0, r0, part, buf, cl,
-                             spl, side, sax, wsum, lb);
+    pss_levels<LOCAL, false>(perm, cent, N, ndim, start, n, p0, r0, part, m, wsum);
 }
 
-static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_local,
-                          int *part_of_elem, BisectWs &ws) {
+static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N, int ndim,
+                          bool do_local, int *part_of_elem, BisectWs &ws) {
   cudaStream_t st = ctx().stream;
   const ll n3 = (ll)ndim * N;
   ws.lists.ensure((size_t)n3);
@@ -1493,13 +1496,13 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, ll N, int ndim, bool do_
       if (do_local) {
         ensure_smem_limit(k_rcb_small_ps<true>, (int)smem);
         k_rcb_small_ps<true><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
-            perm.p, ws.lists.p, ws.loc.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p,
-            t.r0.p, part_of_elem);
+            perm.p, ws.lists.p, ws.loc.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
       } else {
         ensure_smem_limit(k_rcb_small_ps<false>, (int)smem);
         k_rcb_small_ps<false><<<(unsigned)nseg, SMALL_THREADS, smem, st>>>(
-            perm.p, ws.lists.p, ws.loc.p, ws.rank.p, ws.uniq.p, N, ndim, t.start.p, t.n.p, t.p.p,
-            t.r0.p, part_of_elem);
+            perm.p, ws.lists.p, ws.loc.p, cent, N, ndim, t.start.p, t.n.p, t.p.p, t.r0.p,
+            part_of_elem);
       }
       CK_LAUNCH();
       return;
@@ -1611,7 +1614,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
   if (kind == BISECT_RCB && ws.unique) {
     const char *e = getenv("PARRSB_GPU_RCB_PRESORT");
     if (!(e && atoi(e) == 0)) {
-      rcb_presorted(perm, t, N, ndim, do_local, part_of_elem, ws);
+      rcb_presorted(perm, t, cent, N, ndim, do_local, part_of_elem, ws);
       return;
     }
   }
