@@ -1045,18 +1045,6 @@ __global__ void k_ps_side(const int *__restrict__ lists, ll N, const int *__rest
   side[lists[(ll)a * N + j]] = (j - st[s]) >= split[s] ? 1 : 0;
 }
 
-// lower-child flag of list b's entry j (an uncut segment counts as lower:
-// its entries keep their places)
-__device__ __forceinline__ int ps_low(const int *__restrict__ lists, ll N, int b, ll j,
-                                      const int *__restrict__ seg_of_pos,
-                                      const int *__restrict__ axis,
-                                      const unsigned char *__restrict__ side) {
-  if (j >= N) return 0;
-  const int s = seg_of_pos[j];
-  if (axis[s] < 0) return 1;
-  return side[lists[(ll)b * N + j]] == 0 ? 1 : 0;
-}
-
 __device__ __forceinline__ int ps_block_excl(int v, int *total) {
   __shared__ int ws[PS_THREADS / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1084,19 +1072,63 @@ __device__ __forceinline__ int ps_block_excl(int v, int *total) {
   return excl;
 }
 
-// per list (blockIdx.y) and tile of PS_TILE positions: the count of lower flags
+// per tile of PS_TILE positions (PS_TILE / 32 words): the lower-child flags
+// of every list as one bit per position (warp ballots; a position of a
+// segment that is not cut gets 0), each word's count of lower flags before
+// it inside the tile, and the tile's count
+constexpr int PS_WORDS = PS_TILE / 32;
 __global__ void __launch_bounds__(PS_THREADS)
-k_ps_bsum(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
-          const int *__restrict__ axis, const unsigned char *__restrict__ side,
-          int *__restrict__ bsum, int nblk) {
-  const int b = blockIdx.y;
-  const ll j0 = (ll)blockIdx.x * PS_TILE + (ll)threadIdx.x * PS_ITEMS;
-  int c = 0;
+k_ps_flags(const int *__restrict__ lists, ll N, int ndim, const int *__restrict__ seg_of_pos,
+           const int *__restrict__ axis, const unsigned char *__restrict__ side,
+           u32 *__restrict__ bits, int *__restrict__ wpre, int *__restrict__ bsum, int nblk) {
+  __shared__ int wtot[3][PS_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const ll nw = (N + 31) >> 5;
+  const ll w0 = (ll)blockIdx.x * PS_WORDS + (ll)warp * PS_ITEMS;  // this warp's first word
+  bool cut[PS_ITEMS];
 #pragma unroll
-  for (int k = 0; k < PS_ITEMS; k++) c += ps_low(lists, N, b, j0 + k, seg_of_pos, axis, side);
-  int total;
-  ps_block_excl(c, &total);
-  if (threadIdx.x == 0) bsum[(ll)b * nblk + blockIdx.x] = total;
+  for (int r = 0; r < PS_ITEMS; r++) {
+    const ll j = (w0 + r) * 32 + lane;
+    cut[r] = j < N && axis[seg_of_pos[j]] >= 0;
+  }
+  int pre[3][PS_ITEMS];
+#pragma unroll
+  for (int b = 0; b < 3; b++) {
+    if (b >= ndim) break;
+    int c = 0;
+#pragma unroll
+    for (int r = 0; r < PS_ITEMS; r++) {
+      const ll j = (w0 + r) * 32 + lane;
+      const bool f = cut[r] && side[lists[(ll)b * N + j]] == 0;
+      const u32 bal = __ballot_sync(0xffffffffu, f);
+      if (lane == 0 && w0 + r < nw) bits[(ll)b * nw + w0 + r] = bal;
+      pre[b][r] = c;
+      c += __popc(bal);
+    }
+    if (lane == 0) wtot[b][warp] = c;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 3; b++) {
+    if (b >= ndim) break;
+    const int v = wtot[b][lane];  // PS_THREADS / 32 == 32
+    int inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const int base = __shfl_sync(0xffffffffu, inc - v, warp);
+    if (lane < PS_ITEMS && w0 + lane < nw) {
+      int pv = pre[b][0];
+#pragma unroll
+      for (int r = 1; r < PS_ITEMS; r++)
+        if (lane == r) pv = pre[b][r];
+      wpre[(ll)b * nw + w0 + lane] = base + pv;
+    }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    if (threadIdx.x == 0) bsum[(ll)b * nblk + blockIdx.x] = total;
+  }
 }
 
 // per list (blockIdx.x): exclusive scan of its tiles' counts, in place
@@ -1117,42 +1149,40 @@ __global__ void __launch_bounds__(PS_THREADS) k_ps_bscan(int *__restrict__ bsum,
     }
 }
 
-// per list and position: the number of lower flags before it (exclusive)
-__global__ void __launch_bounds__(PS_THREADS)
-k_ps_prefix(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
-            const int *__restrict__ axis, const unsigned char *__restrict__ side,
-            const int *__restrict__ bsum, int nblk, int *__restrict__ clg) {
-  const int b = blockIdx.y;
-  const ll j0 = (ll)blockIdx.x * PS_TILE + (ll)threadIdx.x * PS_ITEMS;
-  int f[PS_ITEMS], c = 0;
-#pragma unroll
-  for (int k = 0; k < PS_ITEMS; k++)
-    f[k] = ps_low(lists, N, b, j0 + k, seg_of_pos, axis, side), c += f[k];
-  int total;
-  int run = ps_block_excl(c, &total) + bsum[(ll)b * nblk + blockIdx.x];
-#pragma unroll
-  for (int k = 0; k < PS_ITEMS; k++) {
-    if (j0 + k < N) clg[(ll)b * N + j0 + k] = run;
-    run += f[k];
-  }
+// lower flags of list b before position x: the tiles before it, the words
+// before it in its tile, the bits below it in its word
+__device__ __forceinline__ ll ps_before(const u32 *__restrict__ bits,
+                                        const int *__restrict__ wpre,
+                                        const int *__restrict__ bsum, ll x) {
+  const ll w = x >> 5;
+  return (ll)bsum[w / PS_WORDS] + wpre[w] + __popc(bits[w] & ((1u << (x & 31)) - 1u));
 }
 
-// stable partition of every cut segment of list b by side
+// stable partition of every cut segment of each list by side, and the
+// segment of every position in the children's table (child_off: the first
+// child of each segment, the lower one of a cut)
 __global__ void k_ps_scatter(const int *__restrict__ lists, ll N, int ndim,
                              const int *__restrict__ seg_of_pos, const ll *__restrict__ st,
                              const int *__restrict__ axis, const ll *__restrict__ split,
-                             const unsigned char *__restrict__ side,
-                             const int *__restrict__ clg, int *__restrict__ lists2) {
+                             const u32 *__restrict__ bits, const int *__restrict__ wpre,
+                             const int *__restrict__ bsum, int nblk,
+                             const ll *__restrict__ child_off, int *__restrict__ lists2,
+                             int *__restrict__ seg_of_pos2) {
   const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= N) return;
   const int s = seg_of_pos[j];
   const ll s0 = st[s];
+  const bool cut = axis[s] >= 0;
+  seg_of_pos2[j] = (int)(child_off[s] + ((cut && j - s0 >= split[s]) ? 1 : 0));
+  const ll nw = (N + 31) >> 5;
   for (int b = 0; b < ndim; b++) {
     const int e = lists[(ll)b * N + j];
     ll dest = j;
-    if (axis[s] >= 0) {
-      const ll c = clg[(ll)b * N + j] - clg[(ll)b * N + s0];  // lower entries before j
-      dest = side[e] == 0 ? s0 + c : s0 + split[s] + (j - s0 - c);
+    if (cut) {
+      const u32 *bb = bits + (ll)b * nw;
+      const int *wp = wpre + (ll)b * nw, *bs = bsum + (ll)b * nblk;
+      const ll c = ps_before(bb, wp, bs, j) - ps_before(bb, wp, bs, s0);  // lower entries before j
+      dest = ((bb[j >> 5] >> (j & 31)) & 1u) ? s0 + c : s0 + split[s] + (j - s0 - c);
     }
     lists2[(ll)b * N + dest] = e;
   }
@@ -1441,7 +1471,6 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
   const ll n3 = (ll)ndim * N;
   ws.lists.ensure((size_t)n3);
   ws.lists2.ensure((size_t)n3);
-  ws.clg.ensure((size_t)n3);
   ws.side.ensure((size_t)N);
   // lists of the initial segments: the global rank order of each axis,
   // grouped stably by segment
@@ -1466,6 +1495,9 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
   CK(cudaMemsetAsync(ws.oax.p, 0xFF, (size_t)t.count * sizeof(int), st));  // -1: input order
   const int nblk = (int)((N + PS_TILE - 1) / PS_TILE);
   ws.bsum.ensure((size_t)ndim * nblk);
+  ws.seg_of_pos2.ensure((size_t)N);
+  ws.pbits.ensure((size_t)ndim * ((N + 31) >> 5));
+  ws.pwpre.ensure((size_t)ndim * ((N + 31) >> 5));
   DBuf<int> nact_d(1);
   DBuf<unsigned long long> maxn_d(1);
   for (int level = 0; level < 200; level++) {
@@ -1483,7 +1515,8 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
     d2h(&nact, nact_d.p, 1);
     d2h(&maxn, maxn_d.p, 1);
     sync();
-    if (level > 0) fill_seg_of_pos(t, ws.seg_of_pos.p, N);
+    // (seg_of_pos follows the table: filled before the loop, then written
+    // for the children by k_ps_scatter)
     if (nact == 0) break;
     if (maxn <= (unsigned long long)SMALL_MAX) {
       // every remaining level in one CTA per segment, on the segment's lists
@@ -1516,23 +1549,25 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
     k_ps_side<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ws.seg_of_pos.p, t.start.p,
                                                 ws.axis.p, ws.split.p, ws.side.p);
     CK_LAUNCH();
-    k_ps_bsum<<<dim3((unsigned)nblk, (unsigned)ndim), PS_THREADS, 0, st>>>(
-        ws.lists.p, N, ws.seg_of_pos.p, ws.axis.p, ws.side.p, ws.bsum.p, nblk);
+    k_ps_flags<<<(unsigned)nblk, PS_THREADS, 0, st>>>(ws.lists.p, N, ndim, ws.seg_of_pos.p,
+                                                      ws.axis.p, ws.side.p, ws.pbits.p,
+                                                      ws.pwpre.p, ws.bsum.p, nblk);
     CK_LAUNCH();
     k_ps_bscan<<<(unsigned)ndim, PS_THREADS, 0, st>>>(ws.bsum.p, nblk);
     CK_LAUNCH();
-    k_ps_prefix<<<dim3((unsigned)nblk, (unsigned)ndim), PS_THREADS, 0, st>>>(
-        ws.lists.p, N, ws.seg_of_pos.p, ws.axis.p, ws.side.p, ws.bsum.p, nblk, ws.clg.p);
-    CK_LAUNCH();
-    k_ps_scatter<<<grid_for(N, 256), 256, 0, st>>>(ws.lists.p, N, ndim, ws.seg_of_pos.p,
-                                                   t.start.p, ws.axis.p, ws.split.p, ws.side.p,
-                                                   ws.clg.p, ws.lists2.p);
+    // children (a cut segment has two, the others one)
+    ws.child_off.ensure((size_t)nseg + 1);
+    exclusive_scan_int_to_ll_async(ws.child_cnt.p, ws.child_off.p, nseg);
+    const ll nchild = nseg + nact;
+    k_ps_scatter<<<grid_for(N, 256), 256, 0, st>>>(
+        ws.lists.p, N, ndim, ws.seg_of_pos.p, t.start.p, ws.axis.p, ws.split.p, ws.pbits.p,
+        ws.pwpre.p, ws.bsum.p, nblk, ws.child_off.p, ws.lists2.p, ws.seg_of_pos2.p);
     CK_LAUNCH();
     std::swap(ws.lists.p, ws.lists2.p);
     std::swap(ws.lists.n, ws.lists2.n);
-    // children, and the list that orders each of them
-    ws.child_off.ensure((size_t)nseg + 1);
-    const ll nchild = exclusive_scan_int_to_ll(ws.child_cnt.p, ws.child_off.p, nseg);
+    std::swap(ws.seg_of_pos.p, ws.seg_of_pos2.p);
+    std::swap(ws.seg_of_pos.n, ws.seg_of_pos2.n);
+    // the children's table, and the list that orders each of them
     ws.t2.reserve(nchild);
     k_children<<<grid_for(nseg, 256), 256, 0, st>>>(
         t.start.p, t.n.p, t.p.p, t.r0.p, nseg, do_local, ws.child_off.p, ws.t2.start.p,

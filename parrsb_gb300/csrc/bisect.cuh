@@ -45,7 +45,10 @@ struct BisectWs {
   // partition scratch
   DBuf<int> sorted;
   bool unique = false;
-  DBuf<int> lists, lists2, clg, oax, oax2, bsum, loc;
+  DBuf<int> lists, lists2, oax, oax2, bsum, loc;
+  DBuf<u32> pbits;  // lower-child flags, one bit per list position
+  DBuf<int> seg_of_pos2;  // the children's segment of every position
+  DBuf<int> pwpre;  // per flag word: lower flags before it in its tile
   DBuf<unsigned char> side;
   DBuf<ll> split;
 };

@@ -73,15 +73,22 @@ __global__ void k_block_scan(const T *in, ll *out, ll n, const ll *boff) {
   }
 }
 
+// want_total = false: the total is not returned (-1) and the host never waits
 template <typename T>
-ll scan_impl(const T *in, ll *out, ll n) {
+ll scan_impl(const T *in, ll *out, ll n, bool want_total = true) {
   cudaStream_t st = ctx().stream;
   if (n <= 0) return 0;
   ll nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   DBuf<ll> bsum((size_t)nb + 1);
+  ll total = -1;
+  if (nb == 1 && !want_total) {
+    CK(cudaMemsetAsync(bsum.p, 0, sizeof(ll), st));  // offset of the only block
+    k_block_scan<T><<<1, SCAN_THREADS, 0, st>>>(in, out, n, bsum.p);
+    CK_LAUNCH();
+    return total;
+  }
   k_block_sums<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, n, bsum.p);
   CK_LAUNCH();
-  ll total;
   if (nb == 1) {
     CK(cudaMemsetAsync(bsum.p + 1, 0, sizeof(ll), st));
     // offset of block 0 is 0; total is bsum[0]
@@ -91,7 +98,7 @@ ll scan_impl(const T *in, ll *out, ll n) {
     total = t0;
     CK(cudaMemsetAsync(bsum.p, 0, sizeof(ll), st));
   } else {
-    total = scan_impl<ll>(bsum.p, bsum.p, nb);
+    total = scan_impl<ll>(bsum.p, bsum.p, nb, want_total);
   }
   k_block_scan<T><<<(unsigned)nb, SCAN_THREADS, 0, st>>>(in, out, n, bsum.p);
   CK_LAUNCH();
@@ -118,6 +125,9 @@ __global__ void k_fill_seg_of_pos(const ll *start, ll nseg, int *seg_of_pos,
 ll exclusive_scan_ll(const ll *in, ll *out, ll n) { return scan_impl<ll>(in, out, n); }
 ll exclusive_scan_int_to_ll(const int *in, ll *out, ll n) {
   return scan_impl<int>(in, out, n);
+}
+void exclusive_scan_int_to_ll_async(const int *in, ll *out, ll n) {
+  scan_impl<int>(in, out, n, false);
 }
 
 void fill_seg_of_pos(const SegTable &t, int *seg_of_pos, ll N) {

@@ -9,6 +9,8 @@ namespace prsb {
 ll exclusive_scan_ll(const ll *in, ll *out, ll n);
 // Same for int inputs; output int64.
 ll exclusive_scan_int_to_ll(const int *in, ll *out, ll n);
+// the same without returning the total: nothing waits on the device
+void exclusive_scan_int_to_ll_async(const int *in, ll *out, ll n);
 
 // Segment table kept on the device (structure of arrays).
 struct SegTable {
