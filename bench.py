@@ -681,7 +681,9 @@ def main():
                              if args.method == "warm" else
                              "learned warm start (network), judged per group the same way"
                              if args.method == "learned" else "the reference's step start"),
-                   "stop": ("restart until the FP64 eigen-residual <= rsb_tol"
+                   "stop": ("restart until the FP64 eigen-residual <= rsb_tol; a pass "
+                            "ends once its Ritz residual bound (checked after steps 3, 6, "
+                            "9, ...) is below 0.7 rsb_tol"
                             if args.method in ("warm", "learned") else
                             "the reference's CG-residual rule"),
                    "learned_start": "see start_vectors.learned_* (network inference cost "

@@ -336,6 +336,10 @@ struct GState {
   int warm;  // start from the learned prediction (else the fallback start)
   int stall;          // residual-stop mode: restarts in a row without progress
   double prev_resid;  //   and the residual of the restart before
+  int stopreq;        // a Ritz residual check asks to end the pass (k_ritz_bound)
+  int rb_it;          //   the step of the group's last computed check in this pass,
+  double rb_theta;    //   its smallest Ritz value and its bound
+  double rb_bound;
 };
 
 __device__ __forceinline__ double block_sum(double v, double *sh) {
@@ -472,6 +476,10 @@ __device__ __forceinline__ void fin_apply(GState &s, int g, double tot0, double 
     s.run = 1;
     s.iters = 0;
     s.done = 0;
+    s.stopreq = 0;
+    s.rb_it = -1;
+    s.rb_theta = 0.0;
+    s.rb_bound = 1e300;
   } else if (OP == FIN_PAP) {
     double pap = tot[0], pap_old = s.pap;
     s.pap = pap;
@@ -500,6 +508,11 @@ __device__ __forceinline__ void fin_apply(GState &s, int g, double tot0, double 
     s.rtz2 = s.rtz1;
     s.rtz1 = rtr;
     s.beta = __ddiv_rn(s.rtz1, s.rtz2);
+    // the off-diagonal that the next step's FIN_PAP enters (the same
+    // expression on the same values), known now for the Ritz residual bound
+    if (owner && it + 1 < MI)
+      upperT[(ll)g * MI + it] =
+          __ddiv_rn(__dmul_rn(-s.beta, s.pap), __dsqrt_rn(__dmul_rn(s.rtz2, s.rtz1)));
   } else if (OP == FIN_PASS_END) {
     s.total_iters += s.iters;
     s.npass += 1;
@@ -1982,14 +1995,15 @@ __device__ __forceinline__ double warp_max_d(double v) {
   return v;
 }
 
-// k-th smallest eigenvalue (0-based) by multisection inside [lo, hi]
+// k-th smallest eigenvalue (0-based) by multisection inside [lo, hi], to a
+// bracket of relative width rel
 __device__ double eig_index(const double *d, const double *e2, int n, int k, double lo,
-                            double hi) {
+                            double hi, double rel = 2.2e-16) {
   const int lane = threadIdx.x;
   double a = lo, b = hi;
   for (int round = 0; round < 24; round++) {
     double w = __dsub_rn(b, a);
-    if (!(w > 2.2e-16 * fmax(fabs(a), fabs(b)) + 1e-300)) break;
+    if (!(w > rel * fmax(fabs(a), fabs(b)) + 1e-300)) break;
     double x = fma(w, (double)(lane + 1) / 33.0, a);
     int cnt = sturm_count(d, e2, n, x);
     unsigned ball = __ballot_sync(0xffffffffu, cnt > k);
@@ -2065,6 +2079,121 @@ __global__ void k_tri_eig(GState *__restrict__ gs, int ngroups,
   __syncwarp();
   for (int j = lane; j < n; j += 32)
     coef[(ll)g * MI + j] = fast_div(x[j], vnorm[(ll)g * (MI + 1) + j]);
+}
+
+// Residual of the current Ritz pair of a running group after step it: with
+// T_k (k = it + 1) the tridiagonal matrix of the pass so far, theta its
+// smallest eigenvalue and y the normalised eigenvector, the Lanczos relation
+// L V_k = V_k T_k + b_k v_(k+1) e_k^T gives |L V_k y - theta V_k y| = |b_k y_k|
+// for an orthonormal basis, b_k = upperT[it] being the off-diagonal that
+// step it + 1 enters (FIN_RTR of step it writes it).  theta by multisection
+// to a relative 1e-10; y_k from the bottom twist of T_k - theta I: the
+// pivots d_i of its LDL^T factorisation (positive below the last for the
+// smallest eigenvalue) and z_(k-1) = 1, z_i = -e_i z_(i+1) / d_i,
+// y_k = 1 / |z|.  Writes the bound to bound_out[g MI + it] (when given) and,
+// when it is below stop_below, asks to end the group's pass (stopreq).
+// It runs on a second stream beside the next steps: it reads only entries
+// of T that step it completed (each written with the same value wherever it
+// is written), whether the group ran step it, and its own fields of the
+// group state, so its answer does not depend on how far the other stream
+// has got; k_apply_stop turns the request into run = 0 at a fixed step after
+// joining the streams.  To spend little of the FP64 pipe, a group whose
+// last bound was above 30 stop_below is computed again only `span` steps
+// after it, and the multisection starts from [0.99 theta', theta'], theta'
+// the last check's Ritz value (the smallest Ritz value never grows with the
+// steps of a pass; both ends are checked by Sturm counts, else Gershgorin's
+// interval).  One warp per group; a group whose T_k has an eigenvalue below
+// 0 is left alone.
+__global__ void k_ritz_bound(GState *__restrict__ gs, int ngroups,
+                             const double *__restrict__ diagT, const double *__restrict__ upperT,
+                             int MI, int it, double stop_below, int span,
+                             double *__restrict__ bound_out) {
+  pdl_entry();
+  extern __shared__ double rb_sm[];
+  const int g = blockIdx.x, lane = threadIdx.x;
+  if (g >= ngroups) return;
+  GState &st = gs[g];
+  if (!st.active || *(volatile const int *)&st.iters < it + 1) return;  // step it not run
+  if (!bound_out && st.rb_it >= 0 && st.rb_bound > 30.0 * stop_below && it - st.rb_it < span)
+    return;  // far from stopping: not yet
+  const int n = it + 1;
+  double *D0 = rb_sm, *E0 = D0 + MI, *e2 = E0 + MI;
+  for (int i = lane; i < n; i += 32) {
+    D0[i] = diagT[(ll)g * MI + i];
+    if (i < n - 1) {
+      const double ev = upperT[(ll)g * MI + i];
+      E0[i] = ev;
+      e2[i] = __dmul_rn(ev, ev);
+    }
+  }
+  __syncwarp();
+  double glo = 1e300, ghi = -1e300;
+  for (int i = lane; i < n; i += 32) {
+    const double r = (i > 0 ? fabs(E0[i - 1]) : 0.0) + (i < n - 1 ? fabs(E0[i]) : 0.0);
+    glo = fmin(glo, __dsub_rn(D0[i], r));
+    ghi = fmax(ghi, __dadd_rn(D0[i], r));
+  }
+  glo = warp_min_d(glo);
+  ghi = warp_max_d(ghi);
+  const double pad = fmax(1e-300, 2.2e-16 * fmax(fabs(glo), fabs(ghi))) * 4.0;
+  glo -= pad, ghi += pad;
+  // lane 0: eigenvalues below 0; lanes 1, 2: the warm bracket's ends
+  const double th0 = st.rb_theta;
+  const double xq = lane == 1 ? 0.99 * th0 : th0;
+  const int cq = (lane == 0 || (th0 > 0.0 && lane < 3)) ? sturm_count(D0, e2, n, lane ? xq : 0.0)
+                                                          : 0;
+  const int c0 = __shfl_sync(0xffffffffu, cq, 0), clo = __shfl_sync(0xffffffffu, cq, 1),
+            chi = __shfl_sync(0xffffffffu, cq, 2);
+  const bool pd = c0 == 0;
+  const bool warm = th0 > 0.0 && clo == 0 && chi >= 1;
+  const double theta =
+      pd ? (warm ? eig_index(D0, e2, n, 0, 0.99 * th0, th0, 1e-10)
+                 : eig_index(D0, e2, n, 0, glo, ghi, 1e-10))
+         : 0.0;
+  if (lane != 0) return;
+  double bound = 1e300;
+  if (pd) {
+    // pivots of T_k - theta I, then z from the bottom (scaled to stay finite)
+    double *dv = e2 + MI;
+    double d = __dsub_rn(D0[0], theta);
+    dv[0] = d;
+    for (int i = 1; i < n; i++) {
+      d = __dsub_rn(__dsub_rn(D0[i], theta), fast_div(e2[i - 1], d));
+      dv[i] = d;
+    }
+    double z = 1.0, zl = 1.0, ss = 1.0;  // current z_i, z_(k-1), sum of squares
+    for (int i = n - 2; i >= 0; i--) {
+      z = fast_div(__dmul_rn(-E0[i], z), dv[i]);
+      if (!(fabs(z) < 1e150)) {
+        if (!isfinite(z)) {  // a zero pivot: the pair is exact to working precision
+          zl = 0.0;
+          ss = 1.0;
+          break;
+        }
+        z = __dmul_rn(z, 1e-150), zl = __dmul_rn(zl, 1e-150), ss = __dmul_rn(ss, 1e-300);
+      }
+      ss = fma(z, z, ss);
+    }
+    const double yk = fast_div(fabs(zl), __dsqrt_rn(ss));
+    bound = __dmul_rn(fabs(upperT[(ll)g * MI + it]), yk);
+  }
+  if (bound_out) bound_out[(ll)g * MI + it] = bound;
+  st.rb_it = it;
+  st.rb_theta = pd ? theta : 0.0;
+  st.rb_bound = bound;
+  if (bound < stop_below) st.stopreq = 1;
+}
+
+// the stop requests of the last Ritz residual check take effect
+__global__ void k_apply_stop(GState *__restrict__ gs, int ngroups) {
+  pdl_entry();
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngroups) return;
+  GState &st = gs[g];
+  if (st.stopreq) {
+    st.run = 0;
+    st.stopreq = 0;
+  }
 }
 
 __global__ void k_set_active(GState *__restrict__ gs, int ngroups) {
@@ -2147,6 +2276,26 @@ struct Lanczos {
   DBuf<ll> fq;                   // fixed-point f of the residual check (FP32)
   DBuf<unsigned> gmax, tmax;     //   each group's and tile's largest |f| (IEEE bits)
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
+  // early pass exit (residual-stop mode): after step it with it + 1 =
+  // early_min + j early_stride, a group whose Ritz residual bound is below
+  // early * rsb_tol ends its pass before step it + early_stride
+  // (k_ritz_bound, k_apply_stop); 0: off
+  double early = 0.0;
+  int early_min = 3, early_stride = 3;
+  bool bound_log = false;        // PARRSB_GPU_PASS_LOG=2: the bound after every step
+  DBuf<double> bnd;              //   [A][MI]
+  cudaStream_t side = nullptr;   // the bound checks' stream, forked from and joined to
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  //   the pass's stream
+  int side_prio = 0;             //   its priority (the device's highest)
+
+  Lanczos() = default;
+  Lanczos(const Lanczos &) = delete;
+  Lanczos &operator=(const Lanczos &) = delete;
+  ~Lanczos() {
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
+  }
   double resid_tol = 0.0;        // its bound (rsb_tol); passes then use
   double cg_factor = 1.0;        //   tol * cg_factor for their own CG exit
   ll VS = 0;                     // row stride of V (N rounded up to 64: 16-byte rows)
@@ -2211,6 +2360,19 @@ struct Lanczos {
     cnt.ensure(A);
     CK(cudaMemsetAsync(cnt.p, 0, (size_t)A * sizeof(int), ctx().stream));
 
+  }
+
+  // a Ritz residual bound after step it (k_ritz_bound); with early exit its
+  // stop requests apply before step it + early_stride (k_apply_stop)
+  bool bound_at(int it) const {
+    if (bound_log) return true;
+    return early > 0.0 && it + 1 >= early_min && (it + 1 - early_min) % early_stride == 0 &&
+           it + early_stride < MI;
+  }
+  int bound_launches() const {
+    int c = 0;
+    for (int it = 0; it < MI; it++) c += bound_at(it) ? 1 : 0;
+    return c * (early > 0.0 ? 2 : 1);
   }
 
   // shared memory of k_tri_eig: 8 arrays of MI doubles and MI ints
@@ -2329,6 +2491,7 @@ struct Lanczos {
   // then 4 MI + 0..5: init start/stop, eig start/stop, ritz start/stop
   void pass_body(const Level &lv, double tol, int mpass, long long *spmv_launches) {
     cudaStream_t st = ctx().stream;
+    bool forked = false;  // bound checks on the side stream (joined at the end)
     mark(4 * MI + 0);
     tile<TM_SUM_F, GATE_ACTIVE>();
     fin<FIN_INIT_MEAN, GATE_ACTIVE>();
@@ -2339,7 +2502,16 @@ struct Lanczos {
       steps_persistent(lv, tol);
       *spmv_launches += MI;
     }
+    int pending = -1;  // step of the bound check whose stop requests are due
     for (int it = 0; it < (persist ? 0 : MI); it++) {
+      if (pending >= 0 && it == pending + early_stride) {  // join, then apply the requests
+        CK(cudaEventRecord(ev_join, side));
+        CK(cudaStreamWaitEvent(st, ev_join, 0));
+        k_apply_stop<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
+        CK_LAUNCH();
+        ctx().kernel_launches++;
+        pending = -1;
+      }
       // three launches per step: each finalises its group scalars in the
       // last tile block of the group
       mark(4 * it + 0);
@@ -2375,6 +2547,28 @@ struct Lanczos {
         }
         fin<FIN_RTR, GATE_RUN>(it, tol, mpass);
       }
+      if (bound_at(it)) {  // on the side stream, beside the next steps
+        CK(cudaEventRecord(ev_fork, st));
+        CK(cudaStreamWaitEvent(side, ev_fork, 0));
+        // (at the highest priority: its blocks take the first free slots
+        // while the step kernels fill the GPU)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)A);
+        cfg.blockDim = dim3(32);
+        cfg.dynamicSmemBytes = (size_t)4 * MI * sizeof(double);
+        cfg.stream = side;
+        cudaLaunchAttribute attr;
+        attr.id = cudaLaunchAttributePriority;
+        attr.val.priority = side_prio;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        CK(cudaLaunchKernelEx(&cfg, k_ritz_bound, gs.p, A, (const double *)diagT.p,
+                              (const double *)upperT.p, MI, it, early * resid_tol,
+                              3 * early_stride, bound_log ? bnd.p : nullptr));
+        ctx().kernel_launches++;
+        forked = true;
+        if (early > 0.0) pending = it;
+      }
       mark(4 * it + 3);
     }
     mark(4 * MI + 2);
@@ -2396,13 +2590,17 @@ struct Lanczos {
       resid2<GATE_ACTIVE>(lv);
       fin<FIN_RESID_GATE, GATE_ACTIVE>(0, resid_tol, mpass);
     }
+    if (forked) {  // every bound check ends before the pass does
+      CK(cudaEventRecord(ev_join, side));
+      CK(cudaStreamWaitEvent(st, ev_join, 0));
+    }
   }
 
   // kernels of the steps of one pass
   long long step_kernels() const {
     if (persist) return 2;
     return (long long)MI * ((pr_fused && !reorth) ? 3 : 5) + (sp_fused ? 0 : MI) +
-           (reorth ? 3ll * MI : 0);
+           (reorth ? 3ll * MI : 0) + bound_launches();
   }
 
   // all steps of the pass in one cooperative launch (k_steps)
@@ -2535,6 +2733,39 @@ struct Lanczos {
       resid_bufs();
       resid_tol = tol;
       tol = tol * cg_factor;  // a pass's own CG exit
+    }
+    // PARRSB_GPU_PASS_LOG=1 (host restart loop): each pass's residuals of the
+    // first groups on stderr; =2 also the Ritz residual bound after every step
+    const int pass_log = [] {
+      const char *v = getenv("PARRSB_GPU_PASS_LOG");
+      return v ? atoi(v) : 0;
+    }();
+    // early pass exit (residual-stop mode only; the persistent step kernel
+    // takes no checks): after steps 3, 6, 9, ... a group whose Ritz residual
+    // bound is below 0.7 rsb_tol ends its pass three steps later (the check
+    // runs beside the next two); the FP64 residual of its Ritz vector still
+    // decides whether it restarts.
+    // PARRSB_GPU_EARLY=<factor> (0: off), _MIN, _STRIDE (at least 2)
+    early = 0.0;
+    if (resid_stop) {
+      early = 0.7, early_min = 3, early_stride = 3;
+      if (const char *v = getenv("PARRSB_GPU_EARLY")) early = std::max(0.0, atof(v));
+      if (const char *v = getenv("PARRSB_GPU_EARLY_MIN")) early_min = std::max(1, atoi(v));
+      // (a request applies before the step of the next check)
+      if (const char *v = getenv("PARRSB_GPU_EARLY_STRIDE")) early_stride = std::max(2, atoi(v));
+    }
+    // (a fused finalisation counts arrivals per group: its tile blocks must
+    // agree on the gate, so no checks run beside it)
+    if (pr_fused || sp_fused) early = 0.0;
+    bound_log = resid_stop && pass_log >= 2 && !pr_fused && !sp_fused;
+    if (bound_log) early = 0.0;  // (the log checks every step and stops nothing)
+    if (bound_log) bnd.ensure((size_t)A * MI);
+    if ((early > 0.0 || bound_log) && !side) {
+      int least = 0;
+      CK(cudaDeviceGetStreamPriorityRange(&least, &side_prio));
+      CK(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, side_prio));
+      CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     }
     // the vectors are scratch until the first pass initialises them
     CK(cudaMemsetAsync(p.p, 0, (size_t)N * sizeof(VT), st));
@@ -2680,6 +2911,8 @@ struct Lanczos {
     const auto hp0 = std::chrono::steady_clock::now();
     for (int pass = 0; pass < mpass; pass++) {
       CK(cudaMemsetAsync(any.p, 0, 2 * sizeof(int), st));
+      if (bound_log)  // 0x7F bytes: a large positive double where no step ran
+        CK(cudaMemsetAsync(bnd.p, 0x7F, (size_t)A * MI * sizeof(double), st));
       if (use_graph) {
         CK(cudaGraphLaunch(exec, st));
         ctx().kernel_launches += per_pass_kernels;
@@ -2693,6 +2926,7 @@ struct Lanczos {
       launches += h_any[1];  // SpMV launches that did work this pass
       ctx().stats.lanczos_passes++;
       npass++;
+      if (pass_log) log_pass(pass);
       if (!ev.empty()) {
         auto el = [&](cudaEvent_t a, cudaEvent_t b) {
           float ms = 0.f;
@@ -2730,6 +2964,35 @@ struct Lanczos {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     finish_run();
+  }
+
+  // one stderr line per group (the first four) after a pass of the host loop
+  void log_pass(int pass) {
+    const int ng = std::min(A, 4);
+    std::vector<GState> h(ng);
+    d2h(h.data(), gs.p, ng);
+    std::vector<double> hb;
+    if (bound_log) {
+      hb.resize((size_t)ng * MI);
+      d2h(hb.data(), bnd.p, hb.size());
+    }
+    sync();
+    const double th[5] = {1e-4, 3e-5, 1e-5, 5e-6, 2e-6};
+    for (int g = 0; g < ng; g++) {
+      fprintf(stderr, "parrsb_gb300: pass %d group %d n=%lld iters=%d resid=%.3e active=%d", pass,
+              g, (long long)h[g].n, h[g].iters, h[g].resid, h[g].active);
+      if (bound_log) {
+        fprintf(stderr, " bound<=[1e-4,3e-5,1e-5,5e-6,2e-6] at");
+        for (double t : th) {
+          int at = -1;
+          for (int it = 0; it < h[g].iters && at < 0; it++)
+            if (hb[(size_t)g * MI + it] <= t) at = it + 1;
+          fprintf(stderr, " %d", at);
+        }
+        if (h[g].iters > 0) fprintf(stderr, " last=%.3e", hb[(size_t)g * MI + h[g].iters - 1]);
+      }
+      fprintf(stderr, "\n");
+    }
   }
 
   // after the restarts: the staged SpMV's error flag, then normalise

@@ -399,9 +399,11 @@ def test_persistent_steps_bitwise(monkeypatch, fp32, mode):
     """All steps of a pass in one cooperative launch (k_steps, grid barriers
     between the phases) give bitwise the partition, the step counts and the
     eigen-residuals of one launch per kernel, inside the device restart
-    loop's graph, in a per-pass graph and without graphs."""
+    loop's graph, in a per-pass graph and without graphs (with the early
+    pass exit off: k_steps runs no Ritz residual checks)."""
     monkeypatch.setenv("PARRSB_GPU_FP32", fp32)
     monkeypatch.setenv("PARRSB_GPU_RESID_STOP", "1")
+    monkeypatch.setenv("PARRSB_GPU_EARLY", "0")
     if mode == "host_loop":
         monkeypatch.setenv("PARRSB_GPU_DEVICE_LOOP", "0")
     if mode == "no_graphs":
@@ -418,6 +420,40 @@ def test_persistent_steps_bitwise(monkeypatch, fp32, mode):
     np.testing.assert_array_equal(out[0][0], out[1][0])
     assert out[0][1:] == out[1][1:]
     assert launches[1] < launches[0] // 2  # the steps ran in k_steps
+
+
+@pytest.mark.parametrize("fp32", ["0", "1"])
+def test_early_pass_exit(monkeypatch, fp32):
+    """Residual-stop mode ends a pass once the Ritz residual bound of a check
+    (after steps 3, 6, 9, ...) is below 0.7 rsb_tol: fewer steps than with
+    the exit off, every FP64-checked residual still at most rsb_tol, a cut
+    within 1% of the full passes' cut, and the same bits on every call and
+    in every launch mode (the checks run on a second stream and their stop
+    requests apply at a fixed step after the streams join)."""
+    monkeypatch.setenv("PARRSB_GPU_FP32", fp32)
+    monkeypatch.setenv("PARRSB_GPU_RESID_STOP", "1")
+    vtx, xyz = meshgen.box_hex(48, 40, 24, jitter=0.1, seed=23)
+    tol = P.default_options().rsb_tol
+
+    def run(**env):
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        part = P.part_mesh(vtx, xyz, 16, partitioner=0)
+        st = P.last_stats()
+        return part, st.lanczos_iters, st.max_fiedler_resid, P.part_quality(part, vtx, 16)[0]
+
+    off = run(PARRSB_GPU_EARLY="0")
+    on = run(PARRSB_GPU_EARLY="0.7")
+    assert on[1] < off[1]
+    assert on[2] <= tol and off[2] <= tol
+    assert abs(on[3] - off[3]) <= 0.01 * off[3]
+    again = run()
+    np.testing.assert_array_equal(on[0], again[0])
+    assert on[1:3] == again[1:3]
+    for env in ({"PARRSB_GPU_DEVICE_LOOP": "0"}, {"PARRSB_GPU_GRAPHS": "0"}):
+        other = run(**env)
+        np.testing.assert_array_equal(on[0], other[0])
+        assert on[1:3] == other[1:3]
 
 
 @pytest.mark.parametrize("fp32", ["0", "1"])
