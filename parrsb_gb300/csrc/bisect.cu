@@ -1215,6 +1215,41 @@ __global__ void k_ps_seg_of_elem(const int *__restrict__ perm, const int *__rest
   if (j < N) seg_of_elem[perm[j]] = seg_of_pos[j];
 }
 
+// The groups of RSB's next level are the halves of this level's (each old
+// group becomes one or two consecutive new segments over its own positions),
+// so the next call's lists are this call's group lists partitioned stably by
+// half.  Per old group: its first child in the new table, whether it has two
+// (axis 0, else -1) and the first child's size; `bad` is set when the new
+// table does not refine the old one that way.
+__global__ void k_inherit_tab(const ll *__restrict__ ost, const ll *__restrict__ on, ll ocount,
+                              const ll *__restrict__ nst, const ll *__restrict__ nn,
+                              const int *__restrict__ nseg_of_pos, int *__restrict__ axis,
+                              ll *__restrict__ split, ll *__restrict__ child_off,
+                              int *__restrict__ bad) {
+  const ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ocount) return;
+  const ll s0 = ost[s], n = on[s];
+  axis[s] = -1, split[s] = n, child_off[s] = 0;
+  if (n <= 0) return;
+  const int c0 = nseg_of_pos[s0], c1 = nseg_of_pos[s0 + n - 1];
+  bool ok = nst[c0] == s0 && (c1 == c0 || c1 == c0 + 1) && nst[c1] + nn[c1] == s0 + n;
+  if (c1 == c0 + 1) ok = ok && nst[c1] == s0 + nn[c0];
+  if (!ok) atomicOr(bad, 1);
+  axis[s] = c1 == c0 + 1 ? 0 : -1;
+  split[s] = nn[c0];
+  child_off[s] = c0;
+}
+
+// side of every element in its old group: 1 for the second child
+__global__ void k_inherit_side(const int *__restrict__ perm, ll N,
+                               const int *__restrict__ oseg_of_pos,
+                               const int *__restrict__ nseg_of_pos,
+                               const ll *__restrict__ child_off, unsigned char *__restrict__ side) {
+  const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  side[perm[j]] = nseg_of_pos[j] != (int)child_off[oseg_of_pos[j]] ? 1 : 0;
+}
+
 __global__ void k_ps_final(const int *__restrict__ lists, ll N, const int *__restrict__ seg_of_pos,
                            const int *__restrict__ oax, int *__restrict__ perm) {
   const ll j = (ll)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1472,13 +1507,55 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
   ws.lists.ensure((size_t)n3);
   ws.lists2.ensure((size_t)n3);
   ws.side.ensure((size_t)N);
+  const int nblk = (int)((N + PS_TILE - 1) / PS_TILE);
+  ws.bsum.ensure((size_t)ndim * nblk);
+  ws.seg_of_pos2.ensure((size_t)N);
+  ws.pbits.ensure((size_t)ndim * ((N + 31) >> 5));
+  ws.pwpre.ensure((size_t)ndim * ((N + 31) >> 5));
   // lists of the initial segments: the global rank order of each axis,
-  // grouped stably by segment
+  // grouped stably by segment; when the segments are the halves of the
+  // previous call's (RSB's next level), that call's lists partitioned by half
   fill_seg_of_pos(t, ws.seg_of_pos.p, N);
+  bool built = false;
   if (t.count == 1) {
     CK(cudaMemcpyAsync(ws.lists.p, ws.sorted.p, (size_t)n3 * sizeof(int),
                        cudaMemcpyDeviceToDevice, st));
-  } else {
+    built = true;
+  } else if (ws.g_ok && ws.g_N == N && ws.g_ndim == ndim && ws.gt.count > 0 &&
+             t.count <= 2 * ws.gt.count) {
+    const ll oc = ws.gt.count;
+    ws.oseg.ensure((size_t)N);
+    fill_seg_of_pos(ws.gt, ws.oseg.p, N);
+    ws.axis.ensure((size_t)oc);
+    ws.split.ensure((size_t)oc);
+    ws.child_off.ensure((size_t)oc + 1);
+    DBuf<int> bad(1);
+    CK(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+    k_inherit_tab<<<grid_for(oc, 256), 256, 0, st>>>(ws.gt.start.p, ws.gt.n.p, oc, t.start.p,
+                                                     t.n.p, ws.seg_of_pos.p, ws.axis.p,
+                                                     ws.split.p, ws.child_off.p, bad.p);
+    CK_LAUNCH();
+    int h_bad = 1;
+    d2h(&h_bad, bad.p, 1);
+    sync();
+    if (!h_bad) {
+      k_inherit_side<<<grid_for(N, 256), 256, 0, st>>>(perm.p, N, ws.oseg.p, ws.seg_of_pos.p,
+                                                       ws.child_off.p, ws.side.p);
+      CK_LAUNCH();
+      k_ps_flags<<<(unsigned)nblk, PS_THREADS, 0, st>>>(ws.glists.p, N, ndim, ws.oseg.p,
+                                                        ws.axis.p, ws.side.p, ws.pbits.p,
+                                                        ws.pwpre.p, ws.bsum.p, nblk);
+      CK_LAUNCH();
+      k_ps_bscan<<<(unsigned)ndim, PS_THREADS, 0, st>>>(ws.bsum.p, nblk);
+      CK_LAUNCH();
+      k_ps_scatter<<<grid_for(N, 256), 256, 0, st>>>(
+          ws.glists.p, N, ndim, ws.oseg.p, ws.gt.start.p, ws.axis.p, ws.split.p, ws.pbits.p,
+          ws.pwpre.p, ws.bsum.p, nblk, ws.child_off.p, ws.lists.p, ws.seg_of_pos2.p);
+      CK_LAUNCH();
+      built = true;
+    }
+  }
+  if (!built) {
     k_ps_seg_of_elem<<<grid_for(N, 256), 256, 0, st>>>(perm.p, ws.seg_of_pos.p, N,
                                                         ws.seg_of_elem.p);
     CK_LAUNCH();
@@ -1491,13 +1568,19 @@ static void rcb_presorted(DBuf<int> &perm, SegTable &t, const double *cent, ll N
                          cudaMemcpyDeviceToDevice, st));
     }
   }
+  // this call's group lists and table, for the next call's lists
+  ws.glists.ensure((size_t)n3);
+  CK(cudaMemcpyAsync(ws.glists.p, ws.lists.p, (size_t)n3 * sizeof(int),
+                     cudaMemcpyDeviceToDevice, st));
+  ws.gt.reserve(t.count);
+  CK(cudaMemcpyAsync(ws.gt.start.p, t.start.p, (size_t)t.count * sizeof(ll),
+                     cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(ws.gt.n.p, t.n.p, (size_t)t.count * sizeof(ll), cudaMemcpyDeviceToDevice,
+                     st));
+  ws.gt.count = t.count;
+  ws.g_ok = true, ws.g_N = N, ws.g_ndim = ndim;
   ws.oax.ensure((size_t)t.count);
   CK(cudaMemsetAsync(ws.oax.p, 0xFF, (size_t)t.count * sizeof(int), st));  // -1: input order
-  const int nblk = (int)((N + PS_TILE - 1) / PS_TILE);
-  ws.bsum.ensure((size_t)ndim * nblk);
-  ws.seg_of_pos2.ensure((size_t)N);
-  ws.pbits.ensure((size_t)ndim * ((N + 31) >> 5));
-  ws.pwpre.ensure((size_t)ndim * ((N + 31) >> 5));
   DBuf<int> nact_d(1);
   DBuf<unsigned long long> maxn_d(1);
   for (int level = 0; level < 200; level++) {
@@ -1644,6 +1727,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
                          cudaMemcpyDeviceToDevice, st));
     }
     ws.rank_of = cent;
+    ws.g_ok = false;  // lists of other centroids
   }
   // PARRSB_GPU_RCB_PRESORT=0: the sort-per-level path even for unique ranks
   if (kind == BISECT_RCB && ws.unique) {
@@ -1653,6 +1737,7 @@ void bisect_segments(BisectKind kind, DBuf<int> &perm, SegTable &t,
       return;
     }
   }
+  ws.g_ok = false;  // the next presorted call builds its lists afresh
   for (int level = 0; level < 200; level++) {
     ll nseg = t.count;
     // active segments, their largest size, and children counts

@@ -48,6 +48,13 @@ struct BisectWs {
   DBuf<int> lists, lists2, oax, oax2, bsum, loc;
   DBuf<u32> pbits;  // lower-child flags, one bit per list position
   DBuf<int> seg_of_pos2;  // the children's segment of every position
+  // the group lists and table of the last presorted call (the next call's
+  // lists when its segments are their halves), and its segment of every position
+  DBuf<int> glists, oseg;
+  SegTable gt;
+  bool g_ok = false;
+  ll g_N = 0;
+  int g_ndim = 0;
   DBuf<int> pwpre;  // per flag word: lower flags before it in its tile
   DBuf<unsigned char> side;
   DBuf<ll> split;
