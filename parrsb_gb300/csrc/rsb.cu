@@ -2278,10 +2278,10 @@ struct Lanczos {
   bool resid_stop = false;       // restarts decided by the FP64 eigen-residual
   // early pass exit (residual-stop mode): after step it with it + 1 =
   // early_min + j early_stride, a group whose Ritz residual bound is below
-  // early * rsb_tol ends its pass before step it + early_stride
-  // (k_ritz_bound, k_apply_stop); 0: off
+  // early * rsb_tol ends its pass before step it + early_delay
+  // (k_ritz_bound, k_apply_stop; 1 <= early_delay <= early_stride); 0: off
   double early = 0.0;
-  int early_min = 3, early_stride = 3;
+  int early_min = 3, early_stride = 3, early_delay = 3;
   bool bound_log = false;        // PARRSB_GPU_PASS_LOG=2: the bound after every step
   DBuf<double> bnd;              //   [A][MI]
   cudaStream_t side = nullptr;   // the bound checks' stream, forked from and joined to
@@ -2363,11 +2363,11 @@ struct Lanczos {
   }
 
   // a Ritz residual bound after step it (k_ritz_bound); with early exit its
-  // stop requests apply before step it + early_stride (k_apply_stop)
+  // stop requests apply before step it + early_delay (k_apply_stop)
   bool bound_at(int it) const {
     if (bound_log) return true;
     return early > 0.0 && it + 1 >= early_min && (it + 1 - early_min) % early_stride == 0 &&
-           it + early_stride < MI;
+           it + early_delay < MI;
   }
   int bound_launches() const {
     int c = 0;
@@ -2504,7 +2504,7 @@ struct Lanczos {
     }
     int pending = -1;  // step of the bound check whose stop requests are due
     for (int it = 0; it < (persist ? 0 : MI); it++) {
-      if (pending >= 0 && it == pending + early_stride) {  // join, then apply the requests
+      if (pending >= 0 && it == pending + early_delay) {  // join, then apply the requests
         CK(cudaEventRecord(ev_join, side));
         CK(cudaStreamWaitEvent(st, ev_join, 0));
         k_apply_stop<<<grid_for(A, 128), 128, 0, st>>>(gs.p, A);
@@ -2751,8 +2751,11 @@ struct Lanczos {
       early = 0.7, early_min = 3, early_stride = 3;
       if (const char *v = getenv("PARRSB_GPU_EARLY")) early = std::max(0.0, atof(v));
       if (const char *v = getenv("PARRSB_GPU_EARLY_MIN")) early_min = std::max(1, atoi(v));
-      // (a request applies before the step of the next check)
-      if (const char *v = getenv("PARRSB_GPU_EARLY_STRIDE")) early_stride = std::max(2, atoi(v));
+      if (const char *v = getenv("PARRSB_GPU_EARLY_STRIDE")) early_stride = std::max(1, atoi(v));
+      // (a request applies at the latest before the step of the next check)
+      early_delay = early_stride;
+      if (const char *v = getenv("PARRSB_GPU_EARLY_DELAY")) early_delay = atoi(v);
+      early_delay = std::max(1, std::min(early_delay, early_stride));
     }
     // (a fused finalisation counts arrivals per group: its tile blocks must
     // agree on the gate, so no checks run beside it)
