@@ -3466,6 +3466,250 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h1).count();
 }
 
+// ----------------------------------------------------------------------------
+// Coarse-graph start (PARRSB_GPU_COARSE=1): for the groups of a level with at
+// least PARRSB_GPU_COARSE_MIN elements, aggregates of 8 consecutive positions
+// of a group (compact in the RCB order of the pre-partition) form a coarse
+// graph with the Laplacian P^T L P (P the aggregation: a coarse row sums its
+// fine rows, entries inside the aggregate cancel in the difference form, an
+// entry's weight is the sum of the fine weights between the two aggregates,
+// split into 4-bit pieces so the coarse matrix is an ordinary level matrix).
+// One Lanczos pass on it from the geometric start, prolonged to the fine
+// positions, becomes the group's warm start candidate (judged as any other).
+// ----------------------------------------------------------------------------
+constexpr int CR_CAP = 512;  // fine entries of one coarse row (8 rows of up to 64)
+
+// fine position -> coarse row (-1 outside the coarse groups)
+__global__ void k_coarse_map(const int *__restrict__ grp, const ll *__restrict__ ast,
+                             const ll *__restrict__ cstart_of, ll N, int *__restrict__ cmap) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int a = grp[i];
+  cmap[i] = (a >= 0 && cstart_of[a] >= 0) ? (int)(cstart_of[a] + (i - ast[a]) / 8) : -1;
+}
+
+// One warp per coarse row: its fine rows' entries (coarse column, weight) in
+// row and slot order, a bitonic sort by (column, weight), the weights summed
+// per column, emitted in column order as pieces of at most 15.  Count mode
+// writes the row's entry count; fill mode writes the entries and the
+// weight-0 padding of its slice.  err: a coarse row had more than CR_CAP
+// fine entries (its extra entries are dropped; the caller then keeps the
+// geometric start).
+template <bool FILL>
+__global__ void __launch_bounds__(256)
+k_coarse_rows(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+              const int *__restrict__ slice_w, const int *__restrict__ cmap,
+              const int *__restrict__ cgrp, const ll *__restrict__ fst,
+              const ll *__restrict__ fn, const ll *__restrict__ cst, ll Nc,
+              int *__restrict__ rowlen, const ll *__restrict__ cslice_off,
+              const int *__restrict__ cslice_w, unsigned *__restrict__ cell,
+              int *__restrict__ err) {
+  __shared__ unsigned long long sbuf[8][CR_CAP];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const ll I = (ll)blockIdx.x * 8 + wib;
+  if (I >= Nc) return;  // the whole warp
+  unsigned long long *buf = sbuf[wib];
+  const int cg = cgrp[I];
+  const ll f0 = fst[cg] + 8 * (I - cst[cg]);
+  const ll f1 = f0 + 8 < fst[cg] + fn[cg] ? f0 + 8 : fst[cg] + fn[cg];
+  int m = 0;
+  for (ll i = f0; i < f1; i++) {
+    const unsigned *ep = ell + slice_off[i >> 5] + (i & 31);
+    const int wd = slice_w[i >> 5];
+    for (int k0 = 0; k0 < wd; k0 += 32) {
+      const int k = k0 + lane;
+      bool ok = false;
+      unsigned long long key = 0;
+      if (k < wd) {
+        const unsigned x = ep[(ll)k * 32];
+        const unsigned w = x >> 28;
+        if (w) {
+          const int J = cmap[x & 0x0FFFFFFFu];
+          if (J >= 0 && (ll)J != I) {
+            ok = true;
+            key = ((unsigned long long)(unsigned)J << 8) | w;
+          }
+        }
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, ok);
+      const int pos = m + __popc(b & ((1u << lane) - 1u));
+      if (ok && pos < CR_CAP) buf[pos] = key;
+      m += __popc(b);
+    }
+  }
+  if (m > CR_CAP) {
+    if (lane == 0) atomicOr(err, 1);
+    m = CR_CAP;
+  }
+  int p2 = 1;
+  while (p2 < m) p2 <<= 1;
+  for (int q = m + lane; q < p2; q += 32) buf[q] = ~0ull;
+  __syncwarp();
+  for (int kk = 2; kk <= p2; kk <<= 1)
+    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+      for (int q = lane; q < p2; q += 32) {
+        const int r = q ^ jj;
+        if (r > q) {
+          const unsigned long long a = buf[q], c = buf[r];
+          if ((q & kk) == 0 ? a > c : a < c) buf[q] = c, buf[r] = a;
+        }
+      }
+      __syncwarp();
+    }
+  if (lane != 0) return;
+  const ll sl = I >> 5;
+  unsigned *out = FILL ? cell + cslice_off[sl] + (I & 31) : nullptr;
+  const int cwd = FILL ? cslice_w[sl] : 0;
+  int e = 0, q = 0;
+  while (q < m) {
+    const unsigned J = (unsigned)(buf[q] >> 8);
+    unsigned W = 0;
+    while (q < m && (unsigned)(buf[q] >> 8) == J) W += (unsigned)(buf[q] & 0xFFu), q++;
+    while (W > 0) {
+      const unsigned c = W > 15u ? 15u : W;
+      if (FILL && e < cwd) out[(ll)e * 32] = J | (c << 28);
+      e++;
+      W -= c;
+    }
+  }
+  if (FILL) {
+    for (; e < cwd; e++) out[(ll)e * 32] = (unsigned)I;  // weight-0 padding
+  } else {
+    rowlen[I] = e;
+  }
+}
+
+// coarse centroids (the mean of the aggregate's) and element spacings (the
+// sums of the aggregate's; only their ratios between axes matter)
+__global__ void k_coarse_cent(const int *__restrict__ perm, const double *__restrict__ cent,
+                              ll nel, const float4 *__restrict__ esp, const int *__restrict__ cgrp,
+                              const ll *__restrict__ fst, const ll *__restrict__ fn,
+                              const ll *__restrict__ cst, ll Nc, double *__restrict__ cent_c,
+                              float4 *__restrict__ esp_c) {
+  const ll I = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= Nc) return;
+  const int cg = cgrp[I];
+  const ll f0 = fst[cg] + 8 * (I - cst[cg]);
+  const ll f1 = f0 + 8 < fst[cg] + fn[cg] ? f0 + 8 : fst[cg] + fn[cg];
+  double sx = 0.0, sy = 0.0, sz = 0.0;
+  float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (ll i = f0; i < f1; i++) {
+    const int el = perm[i];
+    sx += cent[el], sy += cent[nel + el], sz += cent[2 * nel + el];
+    if (esp) {
+      const float4 v = esp[el];
+      q.x += v.x, q.y += v.y, q.z += v.z, q.w += v.w;
+    }
+  }
+  const double inv = 1.0 / (double)(f1 - f0);
+  cent_c[I] = sx * inv, cent_c[Nc + I] = sy * inv, cent_c[2 * Nc + I] = sz * inv;
+  if (esp) esp_c[I] = q;
+}
+
+__global__ void k_coarse_prolong(const int *__restrict__ cmap, const double *__restrict__ fc,
+                                 ll N, double *__restrict__ y) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int c = cmap[i];
+  if (c >= 0) y[i] = fc[c];
+}
+
+__global__ void k_iota_int(int *__restrict__ a, ll n) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = (int)i;
+}
+
+// The coarse start of the level's groups of at least cmin elements (active
+// group a: positions [ast[a], ast[a] + an[a]), grp: active group of every
+// position): y (the geometric start of every group) takes the prolonged
+// coarse Fiedler vector on those groups.  Returns false (y untouched) when
+// no group qualifies or a coarse row overflowed.
+template <typename VT>
+bool coarse_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
+                          const float4 *esp, ll N, int ndim, const std::vector<ll> &ast,
+                          const std::vector<ll> &an, const RsbOpts &o, ll cmin, double *y) {
+  cudaStream_t st = ctx().stream;
+  const int na = (int)ast.size();
+  std::vector<ll> cstart_of(na, -1), fst, fn, cst, cn;
+  std::vector<int> cid;
+  ll Nc = 0;
+  for (int a = 0; a < na; a++) {
+    if (an[a] < cmin || an[a] < 16) continue;
+    cstart_of[a] = Nc;
+    cid.push_back((int)cst.size());
+    fst.push_back(ast[a]), fn.push_back(an[a]);
+    cst.push_back(Nc), cn.push_back((an[a] + 7) / 8);
+    Nc += cn.back();
+  }
+  if (cst.empty()) return false;
+  const int ncg = (int)cst.size();
+  DBuf<ll> d_ast((size_t)na), d_cof((size_t)na), d_fst((size_t)ncg), d_fn((size_t)ncg),
+      d_cst((size_t)ncg);
+  h2d(d_ast.p, ast.data(), (size_t)na);
+  h2d(d_cof.p, cstart_of.data(), (size_t)na);
+  h2d(d_fst.p, fst.data(), (size_t)ncg);
+  h2d(d_fn.p, fn.data(), (size_t)ncg);
+  h2d(d_cst.p, cst.data(), (size_t)ncg);
+  DBuf<int> cmap((size_t)N), cgrp((size_t)Nc), rowlen((size_t)Nc), err(1);
+  k_coarse_map<<<grid_for(N, 256), 256, 0, st>>>(grp, d_ast.p, d_cof.p, N, cmap.p);
+  CK_LAUNCH();
+  fill_groups(cst, cn, cid, cgrp.p, Nc);
+  CK(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+  const unsigned cb = (unsigned)((Nc + 7) / 8);
+  k_coarse_rows<false><<<cb, 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, cmap.p,
+                                           cgrp.p, d_fst.p, d_fn.p, d_cst.p, Nc, rowlen.p,
+                                           nullptr, nullptr, nullptr, err.p);
+  CK_LAUNCH();
+  Level lvc;
+  const ll nslice = (Nc + 31) / 32;
+  DBuf<ll> slots((size_t)nslice + 1);
+  lvc.slice_w.ensure((size_t)nslice);
+  lvc.slice_off.ensure((size_t)nslice + 1);
+  k_slice_w<<<grid_for(nslice, 256), 256, 0, st>>>(rowlen.p, Nc, nslice, slots.p, lvc.slice_w.p);
+  CK_LAUNCH();
+  const ll total = exclusive_scan_ll(slots.p, lvc.slice_off.p, nslice);
+  h2d(lvc.slice_off.p + nslice, &total, 1);
+  lvc.ell.ensure((size_t)total + 32);
+  k_coarse_rows<true><<<cb, 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, cmap.p,
+                                          cgrp.p, d_fst.p, d_fn.p, d_cst.p, Nc, rowlen.p,
+                                          lvc.slice_off.p, lvc.slice_w.p, lvc.ell.p, err.p);
+  CK_LAUNCH();
+  {
+    DBuf<ll> rl64((size_t)Nc);
+    lvc.nnz = exclusive_scan_int_to_ll(rowlen.p, rl64.p, Nc);
+    DBuf<int> mw(1);
+    CK(cudaMemsetAsync(mw.p, 0, sizeof(int), st));
+    k_max_int<<<grid_for(nslice, 256), 256, 0, st>>>(lvc.slice_w.p, nslice, mw.p);
+    CK_LAUNCH();
+    int h_err = 0;
+    d2h(&lvc.max_w, mw.p, 1);
+    d2h(&h_err, err.p, 1);
+    sync();
+    if (h_err) return false;
+  }
+  // coarse centroids, spacings and the geometric start on the coarse graph
+  DBuf<double> cent_c((size_t)3 * Nc), yc((size_t)Nc), fc((size_t)Nc);
+  DBuf<float4> esp_c(esp ? (size_t)Nc : 1);
+  DBuf<int> ident((size_t)Nc);
+  k_iota_int<<<grid_for(Nc, 256), 256, 0, st>>>(ident.p, Nc);
+  CK_LAUNCH();
+  k_coarse_cent<<<grid_for(Nc, 256), 256, 0, st>>>(perm, cent, N, esp, cgrp.p, d_fst.p, d_fn.p,
+                                                   d_cst.p, Nc, cent_c.p,
+                                                   esp ? esp_c.p : nullptr);
+  CK_LAUNCH();
+  geometric_predict_level(lvc, ident.p, cgrp.p, cent_c.p, Nc, ndim, cst, cn, Nc, yc.p, nullptr,
+                          esp ? esp_c.p : nullptr);
+  // one Lanczos pass on the coarse graph
+  RsbOpts oc = o;
+  oc.mpass = 1;
+  Lanczos<VT> lzc;
+  std::vector<GState> resc;
+  run_fiedler_level<VT>(lzc, lvc, oc, cst, cn, Nc, fc.p, resc, yc.p);
+  k_coarse_prolong<<<grid_for(N, 256), 256, 0, st>>>(cmap.p, fc.p, N, y);
+  CK_LAUNCH();
+  return true;
+}
+
 }  // namespace
 
 // ----------------------------------------------------------------------------
@@ -3564,6 +3808,14 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
   BisectWs bws;
   Lanczos<VT> lz;
   Level lv;
+  // coarse-graph start (geometric start mode): groups of at least this many
+  // elements; 0: off
+  const ll coarse_min = [] {
+    const char *e = getenv("PARRSB_GPU_COARSE");
+    if (!(e && atoi(e) != 0)) return (ll)0;
+    const char *m = getenv("PARRSB_GPU_COARSE_MIN");
+    return m ? std::max<ll>(16, atoll(m)) : (ll)1 << 20;
+  }();
   for (int cut = 0; cut < ncuts; cut++) {
     // active groups
     std::vector<ll> ast, an;
@@ -3646,6 +3898,11 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
         else  // start 2: the geometric guess
           geometric_predict_level(lv, perm.p, grp.p, cent, N, ndim, ast, an, N, y_pred.p,
                                   nullptr, esp.p);
+        // PARRSB_GPU_COARSE=1: groups of at least PARRSB_GPU_COARSE_MIN
+        // elements (default 2^20) start from their coarse graph's vector
+        if (!use_net && coarse_min > 0)
+          coarse_predict_level<VT>(lv, perm.p, grp.p, cent, esp.p, N, ndim, ast, an, o,
+                                   coarse_min, y_pred.p);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;
