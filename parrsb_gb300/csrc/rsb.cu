@@ -3468,24 +3468,137 @@ void run_fiedler_level(Lanczos<VT> &lz, const Level &lv, const RsbOpts &o,
 
 // ----------------------------------------------------------------------------
 // Coarse-graph start (PARRSB_GPU_COARSE=1): for the groups of a level with at
-// least PARRSB_GPU_COARSE_MIN elements, aggregates of 8 consecutive positions
-// of a group (compact in the RCB order of the pre-partition) form a coarse
-// graph with the Laplacian P^T L P (P the aggregation: a coarse row sums its
-// fine rows, entries inside the aggregate cancel in the difference form, an
-// entry's weight is the sum of the fine weights between the two aggregates,
-// split into 4-bit pieces so the coarse matrix is an ordinary level matrix).
-// One Lanczos pass on it from the geometric start, prolonged to the fine
-// positions, becomes the group's warm start candidate (judged as any other).
+// least PARRSB_GPU_COARSE_MIN elements, aggregates of elements whose
+// centroids fall in the same cell of two element spacings per axis (on a
+// mesh of near-uniform hexes: blocks of 2x2x2 elements) form a coarse graph
+// with the Laplacian P^T L P (P the aggregation: a coarse row sums its fine
+// rows, entries inside an aggregate cancel in the difference form, an
+// entry's weight is the sum of the fine weights between the two
+// aggregates, split into 4-bit pieces so the coarse matrix is an ordinary
+// level matrix).  One Lanczos pass on it from the geometric start,
+// prolonged to the fine positions, becomes the group's warm start candidate
+// (judged as any other).  A group's spacing per axis is its centroid extent
+// over its number of element layers, round(extent / h) + 1, with h the mean
+// |d| of face neighbours whose displacement lies mostly along that axis.
 // ----------------------------------------------------------------------------
-constexpr int CR_CAP = 512;  // fine entries of one coarse row (8 rows of up to 64)
+constexpr int CR_CAP = 512;  // fine entries of one coarse row
+constexpr int CS_BITS = 14;  // cell index bits per axis in the sort key
 
-// fine position -> coarse row (-1 outside the coarse groups)
-__global__ void k_coarse_map(const int *__restrict__ grp, const ll *__restrict__ ast,
-                             const ll *__restrict__ cstart_of, ll N, int *__restrict__ cmap) {
+// per coarse-eligible group (sel[a] >= 0): ordered-key min / max of the
+// centroid per axis, and per axis the sum and count of |d| over face
+// neighbours (weight wface) displaced mostly along it
+__global__ void k_cs_stats(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
+                           const int *__restrict__ slice_w, const int *__restrict__ perm,
+                           const int *__restrict__ grp, const int *__restrict__ sel,
+                           const double *__restrict__ cent, ll nel, ll N, unsigned wface,
+                           unsigned long long *__restrict__ mn, unsigned long long *__restrict__ mx,
+                           double *__restrict__ hsum, unsigned long long *__restrict__ hcnt) {
+  const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int g = -1;
+  double c[3] = {0.0, 0.0, 0.0}, s[3] = {0.0, 0.0, 0.0};
+  unsigned n[3] = {0u, 0u, 0u};
+  if (i < N) {
+    const int a = grp[i];
+    g = a >= 0 ? sel[a] : -1;
+  }
+  if (g >= 0) {
+    const int e = perm[i];
+    for (int d = 0; d < 3; d++) c[d] = cent[(ll)d * nel + e];
+    const unsigned *ep = ell + slice_off[i >> 5] + (i & 31);
+    const int wd = slice_w[i >> 5];
+    for (int k = 0; k < wd; k++) {
+      const unsigned x = ep[(ll)k * 32];
+      if ((x >> 28) != wface) continue;
+      const int ej = perm[x & 0x0FFFFFFFu];
+      double dd[3], best = -1.0;
+      int ax = 0;
+      for (int d = 0; d < 3; d++) {
+        dd[d] = fabs(cent[(ll)d * nel + ej] - c[d]);
+        if (dd[d] > best) best = dd[d], ax = d;
+      }
+      s[ax] += dd[ax];
+      n[ax] += 1u;
+    }
+  }
+  // one atomic per warp and quantity when the warp lies in one group
+  const int g0 = __shfl_sync(0xffffffffu, g, 0);
+  const bool same = __all_sync(0xffffffffu, g == g0);
+  if (same) {
+    if (g0 < 0) return;
+    for (int d = 0; d < 3; d++) {
+      double v = s[d];
+      unsigned cn = n[d];
+      double lo = c[d], hi = c[d];
+      for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+        cn += __shfl_xor_sync(0xffffffffu, cn, o);
+        lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
+      if (lane == 0) {
+        atomicAdd(&hsum[3 * g0 + d], v);
+        atomicAdd(&hcnt[3 * g0 + d], (unsigned long long)cn);
+        atomicMin(&mn[3 * g0 + d], ordered_key(lo));
+        atomicMax(&mx[3 * g0 + d], ordered_key(hi));
+      }
+    }
+  } else if (g >= 0) {
+    for (int d = 0; d < 3; d++) {
+      atomicAdd(&hsum[3 * g + d], s[d]);
+      atomicAdd(&hcnt[3 * g + d], (unsigned long long)n[d]);
+      atomicMin(&mn[3 * g + d], ordered_key(c[d]));
+      atomicMax(&mx[3 * g + d], ordered_key(c[d]));
+    }
+  }
+}
+
+// sort key of every position: (coarse group, cell z, y, x); ~0 outside
+__global__ void k_cs_keys(const int *__restrict__ perm, const int *__restrict__ grp,
+                          const int *__restrict__ sel, const double *__restrict__ cent, ll nel,
+                          ll N, const double *__restrict__ cmin, const double *__restrict__ ch,
+                          const int *__restrict__ nlay, u64 *__restrict__ keys,
+                          int *__restrict__ vals) {
   const ll i = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int a = grp[i];
-  cmap[i] = (a >= 0 && cstart_of[a] >= 0) ? (int)(cstart_of[a] + (i - ast[a]) / 8) : -1;
+  const int g = a >= 0 ? sel[a] : -1;
+  u64 key = ~0ull;
+  if (g >= 0) {
+    const int e = perm[i];
+    key = (u64)g << (3 * CS_BITS);
+    for (int d = 0; d < 3; d++) {
+      int idx = (int)floor((cent[(ll)d * nel + e] - cmin[3 * g + d]) / ch[3 * g + d] + 0.5);
+      idx = idx < 0 ? 0 : (idx >= nlay[3 * g + d] ? nlay[3 * g + d] - 1 : idx);
+      key |= (u64)(idx >> 1) << (CS_BITS * d);
+    }
+  }
+  keys[i] = key;
+  vals[i] = (int)i;
+}
+
+// runs of equal keys after the sort: flag[s] = 1 at a run's first entry
+__global__ void k_cs_flags(const u64 *__restrict__ keys, ll N, int *__restrict__ flag) {
+  const ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  flag[s] = (keys[s] != ~0ull && (s == 0 || keys[s] != keys[s - 1])) ? 1 : 0;
+}
+
+// aggregate of every position (cmap), each aggregate's first sorted entry
+// (agg_off) and each coarse group's first aggregate (cst_dev)
+__global__ void k_cs_aggs(const u64 *__restrict__ keys, const int *__restrict__ vals,
+                          const int *__restrict__ flag, const ll *__restrict__ excl, ll N,
+                          int *__restrict__ cmap, ll *__restrict__ agg_off,
+                          ll *__restrict__ cst_dev) {
+  const ll s = (ll)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= N || keys[s] == ~0ull) return;
+  const ll agg = excl[s] + flag[s] - 1;
+  cmap[vals[s]] = (int)agg;
+  if (flag[s]) {
+    agg_off[agg] = s;
+    const u64 g = keys[s] >> (3 * CS_BITS);
+    if (s == 0 || (keys[s - 1] >> (3 * CS_BITS)) != g) cst_dev[g] = agg;
+  }
 }
 
 // One warp per coarse row: its fine rows' entries (coarse column, weight) in
@@ -3493,14 +3606,12 @@ __global__ void k_coarse_map(const int *__restrict__ grp, const ll *__restrict__
 // per column, emitted in column order as pieces of at most 15.  Count mode
 // writes the row's entry count; fill mode writes the entries and the
 // weight-0 padding of its slice.  err: a coarse row had more than CR_CAP
-// fine entries (its extra entries are dropped; the caller then keeps the
-// geometric start).
+// fine entries (the caller then keeps the geometric start).
 template <bool FILL>
 __global__ void __launch_bounds__(256)
 k_coarse_rows(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off,
               const int *__restrict__ slice_w, const int *__restrict__ cmap,
-              const int *__restrict__ cgrp, const ll *__restrict__ fst,
-              const ll *__restrict__ fn, const ll *__restrict__ cst, ll Nc,
+              const ll *__restrict__ agg_off, const int *__restrict__ agg_pos, ll Nc,
               int *__restrict__ rowlen, const ll *__restrict__ cslice_off,
               const int *__restrict__ cslice_w, unsigned *__restrict__ cell,
               int *__restrict__ err) {
@@ -3509,11 +3620,9 @@ k_coarse_rows(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off
   const ll I = (ll)blockIdx.x * 8 + wib;
   if (I >= Nc) return;  // the whole warp
   unsigned long long *buf = sbuf[wib];
-  const int cg = cgrp[I];
-  const ll f0 = fst[cg] + 8 * (I - cst[cg]);
-  const ll f1 = f0 + 8 < fst[cg] + fn[cg] ? f0 + 8 : fst[cg] + fn[cg];
   int m = 0;
-  for (ll i = f0; i < f1; i++) {
+  for (ll t = agg_off[I]; t < agg_off[I + 1]; t++) {
+    const ll i = agg_pos[t];
     const unsigned *ep = ell + slice_off[i >> 5] + (i & 31);
     const int wd = slice_w[i >> 5];
     for (int k0 = 0; k0 < wd; k0 += 32) {
@@ -3582,26 +3691,23 @@ k_coarse_rows(const unsigned *__restrict__ ell, const ll *__restrict__ slice_off
 // coarse centroids (the mean of the aggregate's) and element spacings (the
 // sums of the aggregate's; only their ratios between axes matter)
 __global__ void k_coarse_cent(const int *__restrict__ perm, const double *__restrict__ cent,
-                              ll nel, const float4 *__restrict__ esp, const int *__restrict__ cgrp,
-                              const ll *__restrict__ fst, const ll *__restrict__ fn,
-                              const ll *__restrict__ cst, ll Nc, double *__restrict__ cent_c,
-                              float4 *__restrict__ esp_c) {
+                              ll nel, const float4 *__restrict__ esp,
+                              const ll *__restrict__ agg_off, const int *__restrict__ agg_pos,
+                              ll Nc, double *__restrict__ cent_c, float4 *__restrict__ esp_c) {
   const ll I = (ll)blockIdx.x * blockDim.x + threadIdx.x;
   if (I >= Nc) return;
-  const int cg = cgrp[I];
-  const ll f0 = fst[cg] + 8 * (I - cst[cg]);
-  const ll f1 = f0 + 8 < fst[cg] + fn[cg] ? f0 + 8 : fst[cg] + fn[cg];
   double sx = 0.0, sy = 0.0, sz = 0.0;
   float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (ll i = f0; i < f1; i++) {
-    const int el = perm[i];
+  const ll t0 = agg_off[I], t1 = agg_off[I + 1];
+  for (ll t = t0; t < t1; t++) {
+    const int el = perm[agg_pos[t]];
     sx += cent[el], sy += cent[nel + el], sz += cent[2 * nel + el];
     if (esp) {
       const float4 v = esp[el];
       q.x += v.x, q.y += v.y, q.z += v.z, q.w += v.w;
     }
   }
-  const double inv = 1.0 / (double)(f1 - f0);
+  const double inv = 1.0 / (double)(t1 - t0);
   cent_c[I] = sx * inv, cent_c[Nc + I] = sy * inv, cent_c[2 * Nc + I] = sz * inv;
   if (esp) esp_c[I] = q;
 }
@@ -3619,46 +3725,104 @@ __global__ void k_iota_int(int *__restrict__ a, ll n) {
   if (i < n) a[i] = (int)i;
 }
 
-// The coarse start of the level's groups of at least cmin elements (active
-// group a: positions [ast[a], ast[a] + an[a]), grp: active group of every
-// position): y (the geometric start of every group) takes the prolonged
-// coarse Fiedler vector on those groups.  Returns false (y untouched) when
-// no group qualifies or a coarse row overflowed.
+__host__ __device__ inline double key_to_double(unsigned long long k) {
+  const unsigned long long bits = (k >> 63) ? (k ^ 0x8000000000000000ull) : ~k;
+  double d;
+  memcpy(&d, &bits, sizeof d);
+  return d;
+}
+
+// The coarse start of the level's 3D groups of at least cmin elements
+// (active group a: positions [ast[a], ast[a] + an[a]), grp: active group of
+// every position): y (the geometric start of every group) takes the
+// prolonged coarse Fiedler vector on those groups.  Returns false (y
+// untouched) when no group qualifies or a coarse row overflowed.
 template <typename VT>
 bool coarse_predict_level(const Level &lv, const int *perm, const int *grp, const double *cent,
                           const float4 *esp, ll N, int ndim, const std::vector<ll> &ast,
-                          const std::vector<ll> &an, const RsbOpts &o, ll cmin, double *y) {
+                          const std::vector<ll> &an, const RsbOpts &o, ll cmin, double *y,
+                          SortWs &sws) {
   cudaStream_t st = ctx().stream;
+  if (ndim != 3) return false;
   const int na = (int)ast.size();
-  std::vector<ll> cstart_of(na, -1), fst, fn, cst, cn;
-  std::vector<int> cid;
-  ll Nc = 0;
-  for (int a = 0; a < na; a++) {
-    if (an[a] < cmin || an[a] < 16) continue;
-    cstart_of[a] = Nc;
-    cid.push_back((int)cst.size());
-    fst.push_back(ast[a]), fn.push_back(an[a]);
-    cst.push_back(Nc), cn.push_back((an[a] + 7) / 8);
-    Nc += cn.back();
-  }
-  if (cst.empty()) return false;
-  const int ncg = (int)cst.size();
-  DBuf<ll> d_ast((size_t)na), d_cof((size_t)na), d_fst((size_t)ncg), d_fn((size_t)ncg),
-      d_cst((size_t)ncg);
-  h2d(d_ast.p, ast.data(), (size_t)na);
-  h2d(d_cof.p, cstart_of.data(), (size_t)na);
-  h2d(d_fst.p, fst.data(), (size_t)ncg);
-  h2d(d_fn.p, fn.data(), (size_t)ncg);
-  h2d(d_cst.p, cst.data(), (size_t)ncg);
-  DBuf<int> cmap((size_t)N), cgrp((size_t)Nc), rowlen((size_t)Nc), err(1);
-  k_coarse_map<<<grid_for(N, 256), 256, 0, st>>>(grp, d_ast.p, d_cof.p, N, cmap.p);
+  std::vector<int> sel(na, -1), gof;  // coarse group of each active group, and back
+  for (int a = 0; a < na; a++)
+    if (an[a] >= cmin && an[a] >= 64) sel[a] = (int)gof.size(), gof.push_back(a);
+  if (gof.empty()) return false;
+  const int ncg = (int)gof.size();
+  // spacings and extents per group and axis
+  DBuf<int> d_sel((size_t)na);
+  h2d(d_sel.p, sel.data(), (size_t)na);
+  DBuf<unsigned long long> mn((size_t)3 * ncg), mx((size_t)3 * ncg), hcnt((size_t)3 * ncg);
+  DBuf<double> hsum((size_t)3 * ncg);
+  CK(cudaMemsetAsync(mn.p, 0xFF, (size_t)3 * ncg * sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(mx.p, 0, (size_t)3 * ncg * sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(hcnt.p, 0, (size_t)3 * ncg * sizeof(unsigned long long), st));
+  CK(cudaMemsetAsync(hsum.p, 0, (size_t)3 * ncg * sizeof(double), st));
+  k_cs_stats<<<grid_for(N, 256), 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, perm, grp,
+                                               d_sel.p, cent, N, N, 4u, mn.p, mx.p, hsum.p,
+                                               hcnt.p);
   CK_LAUNCH();
+  std::vector<unsigned long long> hmn(3 * ncg), hmx(3 * ncg), hc(3 * ncg);
+  std::vector<double> hs(3 * ncg);
+  d2h(hmn.data(), mn.p, hmn.size());
+  d2h(hmx.data(), mx.p, hmx.size());
+  d2h(hc.data(), hcnt.p, hc.size());
+  d2h(hs.data(), hsum.p, hs.size());
+  sync();
+  std::vector<double> cmin_h(3 * ncg), ch_h(3 * ncg);
+  std::vector<int> nlay(3 * ncg);
+  for (int g = 0; g < ncg; g++)
+    for (int d = 0; d < 3; d++) {
+      const int q = 3 * g + d;
+      const double lo = key_to_double(hmn[q]), hi = key_to_double(hmx[q]);
+      const double ext = hi - lo;
+      const double h = hc[q] ? hs[q] / (double)hc[q] : 0.0;
+      int nl = (h > 0.0 && ext > 0.0) ? (int)std::llround(ext / h) + 1 : 1;
+      if (nl < 1 || nl >= (2 << CS_BITS)) return false;  // too many layers for the key
+      cmin_h[q] = lo;
+      ch_h[q] = nl > 1 ? ext / (double)(nl - 1) : 1.0;
+      nlay[q] = nl;
+    }
+  DBuf<double> d_cmin((size_t)3 * ncg), d_ch((size_t)3 * ncg);
+  DBuf<int> d_nlay((size_t)3 * ncg);
+  h2d(d_cmin.p, cmin_h.data(), cmin_h.size());
+  h2d(d_ch.p, ch_h.data(), ch_h.size());
+  h2d(d_nlay.p, nlay.data(), nlay.size());
+  // aggregates: runs of a sort by (coarse group, cell)
+  DBuf<u64> keys((size_t)N);
+  DBuf<int> vals((size_t)N), flag((size_t)N), cmap((size_t)N), err(1);
+  DBuf<ll> excl((size_t)N), cst_dev((size_t)ncg);
+  k_cs_keys<<<grid_for(N, 256), 256, 0, st>>>(perm, grp, d_sel.p, cent, N, N, d_cmin.p, d_ch.p,
+                                              d_nlay.p, keys.p, vals.p);
+  CK_LAUNCH();
+  seg_sort_pairs(keys, vals, N, nullptr, 1, sws);
+  k_cs_flags<<<grid_for(N, 256), 256, 0, st>>>(keys.p, N, flag.p);
+  CK_LAUNCH();
+  const ll Nc = exclusive_scan_int_to_ll(flag.p, excl.p, N);
+  if (Nc <= 0) return false;
+  DBuf<ll> agg_off((size_t)Nc + 1);
+  CK(cudaMemsetAsync(cmap.p, 0xFF, (size_t)N * sizeof(int), st));
+  k_cs_aggs<<<grid_for(N, 256), 256, 0, st>>>(keys.p, vals.p, flag.p, excl.p, N, cmap.p,
+                                              agg_off.p, cst_dev.p);
+  CK_LAUNCH();
+  ll M = 0;  // eligible positions: the end of the last aggregate
+  for (int g = 0; g < ncg; g++) M += an[gof[g]];
+  h2d(agg_off.p + Nc, &M, 1);
+  std::vector<ll> cst(ncg), cn(ncg);
+  d2h(cst.data(), cst_dev.p, (size_t)ncg);
+  sync();
+  for (int g = 0; g < ncg; g++) cn[g] = (g + 1 < ncg ? cst[g + 1] : Nc) - cst[g];
+  std::vector<int> cid(ncg);
+  for (int g = 0; g < ncg; g++) cid[g] = g;
+  DBuf<int> cgrp((size_t)Nc), rowlen((size_t)Nc);
   fill_groups(cst, cn, cid, cgrp.p, Nc);
+  // coarse level matrix
   CK(cudaMemsetAsync(err.p, 0, sizeof(int), st));
   const unsigned cb = (unsigned)((Nc + 7) / 8);
   k_coarse_rows<false><<<cb, 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, cmap.p,
-                                           cgrp.p, d_fst.p, d_fn.p, d_cst.p, Nc, rowlen.p,
-                                           nullptr, nullptr, nullptr, err.p);
+                                           agg_off.p, vals.p, Nc, rowlen.p, nullptr, nullptr,
+                                           nullptr, err.p);
   CK_LAUNCH();
   Level lvc;
   const ll nslice = (Nc + 31) / 32;
@@ -3671,8 +3835,8 @@ bool coarse_predict_level(const Level &lv, const int *perm, const int *grp, cons
   h2d(lvc.slice_off.p + nslice, &total, 1);
   lvc.ell.ensure((size_t)total + 32);
   k_coarse_rows<true><<<cb, 256, 0, st>>>(lv.ell.p, lv.slice_off.p, lv.slice_w.p, cmap.p,
-                                          cgrp.p, d_fst.p, d_fn.p, d_cst.p, Nc, rowlen.p,
-                                          lvc.slice_off.p, lvc.slice_w.p, lvc.ell.p, err.p);
+                                          agg_off.p, vals.p, Nc, rowlen.p, lvc.slice_off.p,
+                                          lvc.slice_w.p, lvc.ell.p, err.p);
   CK_LAUNCH();
   {
     DBuf<ll> rl64((size_t)Nc);
@@ -3693,9 +3857,8 @@ bool coarse_predict_level(const Level &lv, const int *perm, const int *grp, cons
   DBuf<int> ident((size_t)Nc);
   k_iota_int<<<grid_for(Nc, 256), 256, 0, st>>>(ident.p, Nc);
   CK_LAUNCH();
-  k_coarse_cent<<<grid_for(Nc, 256), 256, 0, st>>>(perm, cent, N, esp, cgrp.p, d_fst.p, d_fn.p,
-                                                   d_cst.p, Nc, cent_c.p,
-                                                   esp ? esp_c.p : nullptr);
+  k_coarse_cent<<<grid_for(Nc, 256), 256, 0, st>>>(perm, cent, N, esp, agg_off.p, vals.p, Nc,
+                                                   cent_c.p, esp ? esp_c.p : nullptr);
   CK_LAUNCH();
   geometric_predict_level(lvc, ident.p, cgrp.p, cent_c.p, Nc, ndim, cst, cn, Nc, yc.p, nullptr,
                           esp ? esp_c.p : nullptr);
@@ -3902,7 +4065,7 @@ static void rsb_impl(const long long *d_vtx, const double *cent, ll N, int nv, i
         // elements (default 2^20) start from their coarse graph's vector
         if (!use_net && coarse_min > 0)
           coarse_predict_level<VT>(lv, perm.p, grp.p, cent, esp.p, N, ndim, ast, an, o,
-                                   coarse_min, y_pred.p);
+                                   coarse_min, y_pred.p, sws);
         CK(cudaEventRecord(w1, st));
         CK(cudaEventSynchronize(w1));
         float ms = 0.f;
